@@ -1,0 +1,113 @@
+"""ORACLE (test infrastructure only): Python bindings of the C restatement.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+use this module.  It loads ``oracle/_build/libfdfk_oracle.so`` (built by
+``make -C oracle``) and exposes:
+
+* :func:`updatedispl` - one restated time step, same arrays as the reference
+  call (src/FDFK2D.f90:516-522);
+* :func:`simulate` - the restated time loop with receiver sampling
+  (src/FDFK2D.f90:465-532);
+* :func:`fd_coef0` / :func:`fd_coef1` / :func:`fd_coef2` (src/Submain.f90:1111-1245).
+
+Array conventions match ``oracle/refharness.py``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libfdfk_oracle.so")
+
+STRIPS = ("uxl_reg", "uzl_reg", "uxr_reg", "uzr_reg", "uxb_reg", "uzb_reg",
+          "uxl_pml", "uzl_pml", "uxr_pml", "uzr_pml", "uxb_pml", "uzb_pml")
+BP = ("bpxlx", "bpzlx", "bpxrx", "bpzrx", "bpxtx", "bpxtz", "bpztx", "bpztz",
+      "bpxbx", "bpxbz", "bpzbx", "bpzbz")
+BU = tuple(f"bu{c}{k}{s}" for s in "lrbt" for c in "xz" for k in "123")
+
+
+class Params(C.Structure):
+    _fields_ = [("norder", C.c_int), ("nx", C.c_int), ("nz", C.c_int), ("npml", C.c_int), ("izt", C.c_int),
+                ("npower", C.c_int), ("nbd", C.c_int), ("nt", C.c_int), ("dx", C.c_float), ("dz", C.c_float),
+                ("dt", C.c_double), ("vpml", C.c_float), ("R0", C.c_double)]
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = C.CDLL(LIB)
+        _lib.fdfk_oracle_updatedispl.restype = C.c_int
+        _lib.fdfk_oracle_simulate.restype = C.c_int
+    return _lib
+
+
+def params(p: dict) -> Params:
+    return Params(int(p["norder"]), int(p["nx"]), int(p["nz"]), int(p["npml"]), int(p["izt"]),
+                  int(p.get("npower", 2)), int(p["nbd"]), int(p["nt"]), float(p["dx"]), float(p["dz"]),
+                  float(p["dt"]), float(p["vpml"]), float(p.get("R0", 1e-3)))
+
+
+def _ptr(a, dtype=np.float32):
+    assert a.dtype == dtype and a.flags.f_contiguous
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _coef(fn, norder):
+    out = np.zeros((norder, norder), np.float64, order="F")
+    getattr(lib(), fn)(C.c_int(norder), _ptr(out, np.float64))
+    return out
+
+
+def fd_coef0(norder):
+    return _coef("fdfk_op_fd_coef0", norder)
+
+
+def fd_coef1(norder):
+    return _coef("fdfk_op_fd_coef1", norder)
+
+
+def fd_coef2(norder):
+    return _coef("fdfk_op_fd_coef2", norder)
+
+
+def updatedispl(p, strips, c, coef0, coef1, ux, uz, bp, bu, it):
+    L = lib()
+    sp = (C.c_void_p * 12)(*[_ptr(strips[k]) for k in STRIPS])
+    bpp = (C.c_void_p * 12)(*[_ptr(bp[k]) for k in BP])
+    bup = (C.c_void_p * 24)(*[_ptr(bu[k]) for k in BU])
+    prm = params(p)
+    rc = L.fdfk_oracle_updatedispl(C.byref(prm), C.c_int(it), sp, _ptr(c), _ptr(coef0, np.float64),
+                                   _ptr(coef1, np.float64), _ptr(ux), _ptr(uz), bpp, bup)
+    if rc != 0:
+        raise RuntimeError(f"oracle updatedispl failed: {rc}")
+
+
+def simulate(p, strips, c, rx, rz, x0, z0, nstp, nsis, steps_limit=-1):
+    """Restated time loop; returns (seisx, seisz) of shape (nsis+1, nrcv), Fortran order."""
+    L = lib()
+    nrcv = len(rx)
+    seisx = np.zeros((nsis + 1, nrcv), np.float32, order="F")
+    seisz = np.zeros((nsis + 1, nrcv), np.float32, order="F")
+    sp = (C.c_void_p * 12)(*[_ptr(strips[k]) for k in STRIPS])
+    rxa = np.asarray(rx, np.float32)
+    rza = np.asarray(rz, np.float32)
+    prm = params(p)
+    rc = L.fdfk_oracle_simulate(C.byref(prm), sp, _ptr(c), C.c_int(nrcv), rxa.ctypes.data_as(C.c_void_p),
+                                rza.ctypes.data_as(C.c_void_p), C.c_float(x0), C.c_float(z0), C.c_int(nstp),
+                                C.c_int(nsis), _ptr(seisx), _ptr(seisz), C.c_int(steps_limit))
+    if rc != 0:
+        raise RuntimeError(f"oracle simulate failed: {rc}")
+    return seisx, seisz
