@@ -1,0 +1,269 @@
+#!/usr/bin/env python3
+"""Benchmark of the FDFK2D hot path on GB300: the hybrid FD-FK time loop.
+
+A step is one time step of the loop of simulate_wavefield (src/FDFK2D.f90:465-532):
+receiver sampling + the fused updatedispl_ step over the whole grid.  The
+workload is the 4001 x 2001 heterogeneous model (config 2: 400 x 200 km at
+100 m, 40-cell PML, FD order 6, 401 receivers) with seeded synthetic inputs.
+
+Prints one JSON line (rank 0).  Arms:
+  default           the GPU path (this repository)
+  --impl reference  the reference's CPU algorithm on this host's cores (the oracle
+                    restatement in oracle/; the reference's own gfortran build
+                    ships x86-64 binaries only)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL_STEP = 36  # read u^n, u^{n-1} (2 comps), write u^{n+1} (2 comps), read rho, lambda, mu: FP32
+METRIC = "Mcell-steps/s"
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM traffic of the step kernel from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "fdfk_step_kernel_config2.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def pinned_strips(w, count, torch):
+    """Pinned host buffers (reference layout, time slowest) holding `count` steps of background."""
+    from fdfk2d_gb300.api import STRIPS, strip_shapes
+    p = w["p"]
+    shp = strip_shapes(p["nx"], p["nz"], p["nbd"], count - 1)
+    bufs, views = {}, {}
+    for k in STRIPS:
+        n1, n2, T = shp[k]
+        t = torch.empty((T, n2, n1), dtype=torch.float32, pin_memory=True)
+        bufs[k] = t
+        views[k] = t.numpy().transpose(2, 1, 0)   # Fortran (n1, n2, T) view
+    return bufs, views
+
+
+def cpu_reference(w, budget_s=15.0, max_steps=40):
+    """The reference algorithm (oracle restatement) on the host cores over a bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from fdfk2d_gb300 import workloads as W
+    p = dict(w["p"], izt=1)
+    cells = (p["nz"] + p["npml"]) * (p["nx"] + 2 * p["npml"])
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+
+    def run(steps):
+        q = dict(p, nt=steps - 1)
+        strips = W.plane_wave_background(dict(w, p=q), 0, steps)
+        t = time.perf_counter()
+        oracle.simulate(q, strips, w["c"], w["rx"], w["rz"], w["x0"], w["z0"], 1, steps - 1, steps_limit=steps)
+        return time.perf_counter() - t
+
+    t1 = run(1)
+    steps = int(max(2, min(max_steps, budget_s / max(t1, 1e-3))))
+    dt = run(steps)
+    value = cells * steps / dt / 1e6
+    return value, cores, f"{steps} time steps of the full {p['nz'] + p['npml']}x{p['nx'] + 2 * p['npml']} grid " \
+                         f"({dt:.1f} s, OMP threads={cores})"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="config2", choices=["config2", "config1"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    K, Wm = args.steps, max(3, args.warmup)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    from fdfk2d_gb300 import workloads as WL
+    w = WL.config2() if args.workload == "config2" else WL.config1()
+    p = w["p"]
+    NZ, NX = p["nz"] + p["npml"], p["nx"] + 2 * p["npml"]
+    cells = NZ * NX
+    config = {"workload": w["name"], "grid": f"{NZ}x{NX} cells incl. PML", "fd_order": 2 * p["norder"],
+              "receivers": len(w["rx"]), "background": "analytic P plane wave on the FK strips (seeded stand-in)",
+              "l2": "state 7 x 33 MB > 129 MB L2 (no flush needed)", "parallelism": f"replicas x{args.gpus}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        value, cores, sample = cpu_reference(w)
+        line = {"metric": METRIC, "value": round(value, 3), "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+                "steps": K, "warmup": Wm, "ms_per_step": round(cells / (value * 1e6) * 1e3, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": config,
+                "cpu_baseline": {"value": round(value, 3), "unit": METRIC, "cores": cores, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": round(value, 3), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    import fdfk2d_gb300 as F
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+
+    # the loop's time axis for this benchmark: warm-up + timed (device-resident) + timed (end to end)
+    total = Wm + 2 * K
+    q = dict(p, nt=total - 1)
+    wq = dict(w, p=q)
+    bufs, host = pinned_strips(wq, total, torch)
+    WL.plane_wave_background(wq, 0, total, out=host)
+    sess = F.Session(q, w["c"], stream=stream.cuda_stream)
+    sess.set_receivers(w["rx"], w["rz"], w["x0"], w["z0"], 1, total - 1)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident arm: inputs in HBM before the timed region
+    sess.upload_background(host, 0, Wm + K)
+    sess.advance(Wm)
+    sess.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    n0 = F.kernel_launches()
+    e0.record(stream)
+    sess.advance(K)
+    e1.record(stream)
+    barrier()
+    launches = F.kernel_launches() - n0
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    t_dev = torch.tensor([ms], device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t_dev, op=torch.distributed.ReduceOp.MAX)
+    ms = float(t_dev.item())
+    ms_step = ms / K
+    value = cells * K * world / (ms / 1e3) / 1e6
+
+    # ---- end-to-end arm: host (pinned) background in, seismograms out, through the C ABI
+    outx = np.zeros((K, len(w["rx"])), np.float32, order="F")
+    outz = np.zeros_like(outx, order="F")
+    barrier()
+    t0 = time.perf_counter()
+    sess.upload_background(host, Wm + K, K)
+    sess.advance(K)
+    sess.seismogram_range(Wm + K, K, outx, outz)
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    e2e_value = cells * K * world / t_e2e / 1e6
+    h2d = sum(int(np.prod(host[k].shape[:2])) for k in F.STRIPS) * 4
+    d2h = len(w["rx"]) * 2 * 4
+    assert np.isfinite(outz).all()
+    sess.close()
+
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_CELL_STEP * cells / (ms_step / 1e3) / 1e9
+    traffic = profile_traffic()
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        value_cpu, cores, sample = cpu_reference(w)
+        cpu = {"value": round(value_cpu, 3), "unit": METRIC, "cores": cores, "kind": "port", "sample": sample}
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 1), "unit": METRIC, "n_gpus": world, "steps": K, "warmup": Wm,
+                "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic", "config": config,
+                "e2e": {"value": round(e2e_value, 1), "unit": METRIC, "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "gpu_launches": int(launches),
+                "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                             "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+                             "bytes_per_cell_step": BYTES_PER_CELL_STEP},
+                "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,20 @@
+"""fdfk2d_gb300: GB300 (sm_103a) hot path of FDFK2D's hybrid FD-FK solver.
+
+The compute runs in ``_build/libfdfk_gb300.so`` (hand-written CUDA, C ABI in
+``include/fdfk_gb300.h``); this package is its host-side mirror of the
+reference interface:
+
+* :func:`updatedispl` - the reference's per-step entry point
+  (``updatedispl_``, src/FDFK2D.f90:516-522), same arrays, same in-place update;
+* :class:`Session` - device-resident solver state for the time loop of
+  ``simulate_wavefield`` (src/FDFK2D.f90:465-532);
+* :func:`simulate` - the whole time loop in one call (host arrays in, seismograms out).
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is
+visible, calls raise.
+"""
+from .api import (FDFKError, Params, Session, STRIPS, BP, BU, lib, lib_path, simulate, strip_shapes,
+                  pml_shapes, updatedispl, kernel_launches)
+
+__all__ = ["FDFKError", "Params", "Session", "STRIPS", "BP", "BU", "lib", "lib_path", "simulate",
+           "strip_shapes", "pml_shapes", "updatedispl", "kernel_launches"]

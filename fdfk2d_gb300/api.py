@@ -1,0 +1,228 @@
+"""ctypes binding of the C ABI (include/fdfk_gb300.h) with the reference's array conventions.
+
+Arrays are numpy arrays in Fortran order with the shapes the reference
+allocates (src/FDFK2D.f90:253-355):
+
+* ``c``: ``(3, nz+npml, nx+2*npml)`` = rho, lambda, mu (src/FDFK2D.f90:125)
+* ``ux``, ``uz``: ``(2, nz+npml, nx+2*npml)``; level 1 = u^n, level 2 = u^{n-1}
+* background strips: dict name -> ``(n1, n2, nt+1)`` float32, names in :data:`STRIPS`
+* PML state: dicts over :data:`BP` / :data:`BU` with :func:`pml_shapes`
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+
+STRIPS = ("uxl_reg", "uzl_reg", "uxr_reg", "uzr_reg", "uxb_reg", "uzb_reg",
+          "uxl_pml", "uzl_pml", "uxr_pml", "uzr_pml", "uxb_pml", "uzb_pml")
+BP = ("bpxlx", "bpzlx", "bpxrx", "bpzrx", "bpxtx", "bpxtz", "bpztx", "bpztz",
+      "bpxbx", "bpxbz", "bpzbx", "bpzbz")
+BU = tuple(f"bu{c}{k}{s}" for s in "lrbt" for c in "xz" for k in "123")
+
+STATUS = {0: "ok", -1: "invalid argument", -2: "unsupported", -3: "out of memory", -4: "CUDA error",
+          -5: "call out of order"}
+
+
+class FDFKError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"fdfk_gb300: {STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    """fdfk_params: scalar arguments of updatedispl_ (src/FDFK2D.f90:516-519)."""
+    _fields_ = [("norder", C.c_int), ("nx", C.c_int), ("nz", C.c_int), ("npml", C.c_int),
+                ("is_PML_top", C.c_int), ("npower", C.c_int), ("nbd", C.c_int), ("nt", C.c_int),
+                ("dx", C.c_float), ("dz", C.c_float), ("dt", C.c_double), ("vpml", C.c_float),
+                ("R0", C.c_double)]
+
+    @classmethod
+    def from_dict(cls, p: dict) -> "Params":
+        return cls(int(p["norder"]), int(p["nx"]), int(p["nz"]), int(p["npml"]), int(bool(p.get("is_PML_top", False))),
+                   int(p.get("npower", 2)), int(p.get("nbd", 2 * int(p["norder"]) - 1)), int(p["nt"]),
+                   float(p["dx"]), float(p["dz"]), float(p["dt"]), float(p["vpml"]), float(p.get("R0", 1e-3)))
+
+
+def lib_path() -> str:
+    return os.path.join(PKG, "_build", "libfdfk_gb300.so")
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (fails loudly if it was not built)."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            raise ImportError(f"fdfk_gb300 CUDA library not built: {path} (run __graft_entry__.build())")
+        L = C.CDLL(path)
+        L.fdfk_last_error.restype = C.c_char_p
+        L.fdfk_kernel_launches.restype = C.c_longlong
+        L.fdfk_session_create.argtypes = [C.POINTER(Params), C.c_void_p, C.POINTER(C.c_void_p)]
+        for name in ("fdfk_session_set_stream", "fdfk_session_advance", "fdfk_session_synchronize",
+                     "fdfk_session_step_index", "fdfk_session_destroy", "fdfk_session_upload_background",
+                     "fdfk_session_set_receivers", "fdfk_session_download_seismograms",
+                     "fdfk_session_upload_state", "fdfk_session_download_state",
+                     "fdfk_session_download_seismogram_range"):
+            getattr(L, name).restype = C.c_int if name != "fdfk_session_destroy" else None
+        _lib = L
+    return _lib
+
+
+def kernel_launches() -> int:
+    return int(lib().fdfk_kernel_launches())
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise FDFKError(rc, lib().fdfk_last_error().decode())
+
+
+def _f32(a, name):
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.f_contiguous):
+        raise TypeError(f"{name} must be a Fortran-ordered float32 array")
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def strip_shapes(nx, nz, nbd, nt):
+    """Background-strip shapes, src/FDFK2D.f90:328-355 (last axis = time 0..nt)."""
+    T = nt + 1
+    return {"uxl_reg": (nz - nbd, nbd, T), "uzl_reg": (nz - nbd, nbd, T),
+            "uxr_reg": (nz - nbd, nbd, T), "uzr_reg": (nz - nbd, nbd, T),
+            "uxb_reg": (nbd, nx, T), "uzb_reg": (nbd, nx, T),
+            "uxl_pml": (nz, nbd, T), "uzl_pml": (nz, nbd, T),
+            "uxr_pml": (nz, nbd, T), "uzr_pml": (nz, nbd, T),
+            "uxb_pml": (nbd, nx + 2 * nbd, T), "uzb_pml": (nbd, nx + 2 * nbd, T)}
+
+
+def pml_shapes(nx, nz, npml):
+    """PML auxiliary-array shapes, src/FDFK2D.f90:260-306."""
+    X = nx + 2 * npml
+    s = {"bpxlx": (nz, npml), "bpzlx": (nz, npml), "bpxrx": (nz, npml), "bpzrx": (nz, npml)}
+    for k in ("bpxtx", "bpxtz", "bpztx", "bpztz", "bpxbx", "bpxbz", "bpzbx", "bpzbz"):
+        s[k] = (npml, X)
+    for name in BU:
+        s[name] = (2, nz, npml) if name[-1] in "lr" else (2, npml, X)
+    return s
+
+
+class Session:
+    """Device-resident time loop of simulate_wavefield (src/FDFK2D.f90:465-532)."""
+
+    def __init__(self, p: dict, c: np.ndarray, stream=None):
+        L = lib()
+        self.p = dict(p)
+        self._prm = Params.from_dict(p)
+        h = C.c_void_p()
+        _check(L.fdfk_session_create(C.byref(self._prm), _f32(c, "c"), C.byref(h)))
+        self._h = h
+        self.nrcv = 0
+        self.nsis = -1
+        if stream is not None:
+            _check(L.fdfk_session_set_stream(self._h, C.c_void_p(int(stream))))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fdfk_session_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def upload_background(self, strips: dict, t0: int = 0, count: int | None = None):
+        if count is None:
+            count = int(self.p["nt"]) + 1 - t0
+        arr = (C.c_void_p * 12)(*[_f32(strips[k], k) for k in STRIPS])
+        _check(lib().fdfk_session_upload_background(self._h, arr, C.c_int(t0), C.c_int(count)))
+
+    def set_receivers(self, rx, rz, x0: float, z0: float, nstp: int, nsis: int):
+        rx = np.ascontiguousarray(rx, np.float32)
+        rz = np.ascontiguousarray(rz, np.float32)
+        _check(lib().fdfk_session_set_receivers(self._h, C.c_int(len(rx)), rx.ctypes.data_as(C.c_void_p),
+                                                 rz.ctypes.data_as(C.c_void_p), C.c_float(x0), C.c_float(z0),
+                                                 C.c_int(nstp), C.c_int(nsis)))
+        self.nrcv, self.nsis = len(rx), nsis
+
+    def advance(self, nsteps: int):
+        _check(lib().fdfk_session_advance(self._h, C.c_int(nsteps)))
+
+    @property
+    def step_index(self) -> int:
+        return int(lib().fdfk_session_step_index(self._h))
+
+    def synchronize(self):
+        _check(lib().fdfk_session_synchronize(self._h))
+
+    def seismograms(self):
+        sx = np.zeros((self.nsis + 1, self.nrcv), np.float32, order="F")
+        sz = np.zeros_like(sx, order="F")
+        _check(lib().fdfk_session_download_seismograms(self._h, _f32(sx, "seisx"), _f32(sz, "seisz")))
+        return sx, sz
+
+    def seismogram_range(self, first: int, count: int, outx=None, outz=None):
+        """Samples [first, first+count) of every receiver, arrays of shape (count, nrcv)."""
+        sx = outx if outx is not None else np.zeros((count, self.nrcv), np.float32, order="F")
+        sz = outz if outz is not None else np.zeros((count, self.nrcv), np.float32, order="F")
+        _check(lib().fdfk_session_download_seismogram_range(self._h, C.c_int(first), C.c_int(count),
+                                                             _f32(sx, "seisx"), _f32(sz, "seisz")))
+        return sx, sz
+
+    def upload_state(self, ux, uz, bp: dict, bu: dict, it: int):
+        bpp = (C.c_void_p * 12)(*[_f32(bp[k], k) if k in bp else None for k in BP])
+        bup = (C.c_void_p * 24)(*[_f32(bu[k], k) if k in bu else None for k in BU])
+        _check(lib().fdfk_session_upload_state(self._h, _f32(ux, "ux"), _f32(uz, "uz"), bpp, bup, C.c_int(it)))
+
+    def download_state(self, ux, uz, bp: dict, bu: dict):
+        bpp = (C.c_void_p * 12)(*[_f32(bp[k], k) if k in bp else None for k in BP])
+        bup = (C.c_void_p * 24)(*[_f32(bu[k], k) if k in bu else None for k in BU])
+        _check(lib().fdfk_session_download_state(self._h, _f32(ux, "ux"), _f32(uz, "uz"), bpp, bup))
+
+
+def simulate(p: dict, c: np.ndarray, strips: dict, rx, rz, x0: float, z0: float, nstp: int, nsis: int):
+    """The whole time loop on the GPU; returns (seisx, seisz) of shape (nsis+1, nrcv)."""
+    L = lib()
+    prm = Params.from_dict(p)
+    rx = np.ascontiguousarray(rx, np.float32)
+    rz = np.ascontiguousarray(rz, np.float32)
+    sx = np.zeros((nsis + 1, len(rx)), np.float32, order="F")
+    sz = np.zeros_like(sx, order="F")
+    arr = (C.c_void_p * 12)(*[_f32(strips[k], k) for k in STRIPS])
+    _check(L.fdfk_simulate(C.byref(prm), _f32(c, "c"), arr, C.c_int(len(rx)), rx.ctypes.data_as(C.c_void_p),
+                           rz.ctypes.data_as(C.c_void_p), C.c_float(x0), C.c_float(z0), C.c_int(nstp),
+                           C.c_int(nsis), _f32(sx, "seisx"), _f32(sz, "seisz")))
+    return sx, sz
+
+
+def updatedispl(p: dict, strips: dict, c, coef0, coef1, ux, uz, bp: dict, bu: dict, it: int):
+    """The reference entry point updatedispl_ (68 arguments), executed on the GPU in place."""
+    L = lib()
+    i = lambda v: C.byref(C.c_int(int(v)))
+    f = lambda v: C.byref(C.c_float(float(v)))
+    d = lambda v: C.byref(C.c_double(float(v)))
+    norder = int(p["norder"])
+    izt = 1 - int(p["npml"]) if p.get("is_PML_top", False) else 1
+    args = [i(norder), i(p["nx"]), i(p["nz"]), i(p["npml"]), i(izt), i(1 if p.get("is_PML_top", False) else 0),
+            i(p.get("npower", 2)), i(p.get("nbd", 2 * norder - 1)), i(it), i(p["nt"]), f(p["dx"]), f(p["dz"]),
+            d(p["dt"]), f(p["vpml"]), d(p.get("R0", 1e-3))]
+    args += [_f32(strips[k], k) for k in STRIPS]
+    c0 = np.asfortranarray(coef0, np.float64)
+    c1 = np.asfortranarray(coef1, np.float64)
+    args += [_f32(c, "c"), c0.ctypes.data_as(C.c_void_p), c1.ctypes.data_as(C.c_void_p), _f32(ux, "ux"), _f32(uz, "uz")]
+    args += [_f32(bp[k], k) for k in BP]
+    args += [_f32(bu[k], k) for k in BU]
+    L.updatedispl_(*args)

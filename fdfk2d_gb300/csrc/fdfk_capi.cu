@@ -1,0 +1,605 @@
+// C ABI of fdfk_gb300: sessions, the one-shot time loop and the gfortran-ABI
+// drop-in `updatedispl_`.  Declarations and contracts: include/fdfk_gb300.h.
+#include "fdfk_gb300.h"
+#include "fdfk_sweep.cuh"
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace fdfk {
+cudaError_t launch_step(const StepArgs& a, cudaStream_t s);
+cudaError_t set_coefficients(const float* stag, const float* coll);
+size_t step_smem_bytes(int norder);
+}  // namespace fdfk
+
+using namespace fdfk;
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<long long> g_launches{0};
+
+int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return fail(FDFK_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Staggered (fd_coef0) and collocated (fd_coef1) first-derivative weights for
+// every reduced order n = 1..8 (src/Submain.f90:1111-1200): the weights of the
+// order-2n centred difference on a staggered / collocated stencil.
+void fd_tables(float stag[kMaxOrder + 1][kMaxOrder + 1], float coll[kMaxOrder + 1][kMaxOrder + 1])
+{
+    for (int n = 0; n <= kMaxOrder; ++n)
+        for (int j = 0; j <= kMaxOrder; ++j) stag[n][j] = coll[n][j] = 0.f;
+    for (int n = 1; n <= kMaxOrder; ++n) {
+        for (int j = 1; j <= n; ++j) {
+            // staggered: nodes at odd half-integers (2k-1)/2
+            double num = 1.0, den = 1.0;
+            const double aj = (double)((2 * j - 1) * (2 * j - 1));
+            for (int k = 1; k <= n; ++k) {
+                if (k == j) continue;
+                const double ak = (double)((2 * k - 1) * (2 * k - 1));
+                num *= ak;
+                den *= (k < j) ? (aj - ak) : (ak - aj);
+            }
+            double sgn = (j % 2 == 1) ? 1.0 : -1.0;
+            stag[n][j] = (float)(sgn * num / (den * (double)(2 * j - 1)));
+            // collocated: nodes at integers k
+            double numc = 1.0, denc = 1.0;
+            const double bj = (double)(j * j);
+            for (int k = 1; k <= n; ++k) {
+                if (k == j) continue;
+                const double bk = (double)(k * k);
+                numc *= bk;
+                denc *= (k < j) ? (bj - bk) : (bk - bj);
+            }
+            coll[n][j] = (float)(sgn * numc / (denc * 2.0 * (double)j));
+        }
+    }
+}
+
+size_t strip_elems(const fdfk_params& p, int k)
+{
+    const size_t nx = p.nx, nz = p.nz, nbd = p.nbd;
+    switch (k) {
+    case UXL_REG: case UZL_REG: case UXR_REG: case UZR_REG: return (nz - nbd) * nbd;
+    case UXB_REG: case UZB_REG: return nbd * nx;
+    case UXL_PML: case UZL_PML: case UXR_PML: case UZR_PML: return nz * nbd;
+    default: return nbd * (nx + 2 * nbd);
+    }
+}
+
+// bu / bp array sizes (elements per plane) in the updatedispl_ argument order.
+size_t bu_elems(const fdfk_params& p, int k)
+{
+    const size_t side = (size_t)p.nz * p.npml, tb = (size_t)p.npml * (p.nx + 2 * p.npml);
+    return k < 12 ? side : tb;   // l, r then b, t
+}
+size_t bp_elems(const fdfk_params& p, int k)
+{
+    const size_t side = (size_t)p.nz * p.npml, tb = (size_t)p.npml * (p.nx + 2 * p.npml);
+    return k < 4 ? side : tb;
+}
+
+}  // namespace
+
+struct fdfk_session {
+    fdfk_params p{};
+    int NZ = 0, NX = 0, ldz = 0;
+    cudaStream_t stream = nullptr;
+    float* kdt2 = nullptr;
+    float* lam = nullptr;
+    float* mu = nullptr;
+    float* ux[2] = {nullptr, nullptr};
+    float* uz[2] = {nullptr, nullptr};
+    float* bu[24][2] = {};
+    float* bp[12] = {};
+    DampCol* dampx = nullptr;
+    DampCol* dampz = nullptr;
+    float* strip[NSTRIP] = {};
+    std::vector<char> have_bg;   // per time index
+    int cur = 0;
+    int it = 0;
+    // receivers
+    int nrcv = 0, nstp = 1, nsis = -1, isis = 0, istp = 0;
+    float x0 = 0.f, z0 = 0.f;
+    float* rx = nullptr;
+    float* rz = nullptr;
+    float* seisx = nullptr;
+    float* seisz = nullptr;
+    StepArgs base{};
+};
+
+namespace {
+
+int validate(const fdfk_params* p)
+{
+    if (!p) return fail(FDFK_EINVAL, "params is NULL");
+    if (p->is_PML_top) return fail(FDFK_EUNSUPPORTED, "is_PML_top: only the free-surface top boundary is implemented");
+    if (p->norder < 1 || p->norder > kMaxOrder) return fail(FDFK_EINVAL, "norder must be 1..8");
+    if (p->nbd != 2 * p->norder - 1) return fail(FDFK_EINVAL, "nbd must equal 2*norder-1");
+    if (p->npml < p->nbd) return fail(FDFK_EINVAL, "npml must be >= 2*norder-1");
+    if (p->nx < 1 || p->nz <= p->nbd + 1) return fail(FDFK_EINVAL, "grid too small (need nx >= 1, nz > nbd+1)");
+    if (p->nx < 2 * p->nbd) return fail(FDFK_EINVAL, "nx must be >= 2*nbd");
+    if (p->nt < 0) return fail(FDFK_EINVAL, "nt must be >= 0");
+    if (!(p->dx > 0.f) || !(p->dz > 0.f) || !(p->dt > 0.0)) return fail(FDFK_EINVAL, "dx, dz, dt must be positive");
+    if (!(p->R0 > 0.0) || !(p->R0 < 1.0)) return fail(FDFK_EINVAL, "R0 must be in (0, 1)");
+    if ((double)(p->nz + p->npml) * (p->nx + 2 * p->npml) > 2.0e9) return fail(FDFK_EINVAL, "grid too large");
+    return FDFK_OK;
+}
+
+void free_session(fdfk_session* s)
+{
+    if (!s) return;
+    cudaFree(s->kdt2); cudaFree(s->lam); cudaFree(s->mu);
+    for (int l = 0; l < 2; ++l) { cudaFree(s->ux[l]); cudaFree(s->uz[l]); }
+    for (int k = 0; k < 24; ++k) for (int l = 0; l < 2; ++l) cudaFree(s->bu[k][l]);
+    for (int k = 0; k < 12; ++k) cudaFree(s->bp[k]);
+    cudaFree(s->dampx); cudaFree(s->dampz);
+    for (int k = 0; k < NSTRIP; ++k) cudaFree(s->strip[k]);
+    cudaFree(s->rx); cudaFree(s->rz); cudaFree(s->seisx); cudaFree(s->seisz);
+    delete s;
+}
+
+int upload_material(fdfk_session* s, const float* c)
+{
+    const fdfk_params& p = s->p;
+    const size_t n = (size_t)s->ldz * s->NX;
+    std::vector<float> k(n, 0.f), l(n, 0.f), m(n, 1.f);
+    const double dt2 = p.dt * p.dt;
+    for (int x = 0; x < s->NX; ++x)
+        for (int z = 0; z < s->NZ; ++z) {
+            size_t src = 3 * ((size_t)z + (size_t)s->NZ * x);
+            size_t dst = (size_t)z + (size_t)s->ldz * x;
+            if (!(c[src] > 0.f)) return fail(FDFK_EINVAL, "density must be positive everywhere");
+            k[dst] = (float)(dt2 / (double)c[src]);
+            l[dst] = c[src + 1];
+            m[dst] = c[src + 2];
+            if (!(m[dst] > 0.f) || !(l[dst] + 2.0f * m[dst] > 0.f))
+                return fail(FDFK_EINVAL, "mu and lambda+2mu must be positive everywhere");
+        }
+    CK(cudaMemcpyAsync(s->kdt2, k.data(), n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->lam, l.data(), n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->mu, m.data(), n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FDFK_OK;
+}
+
+// Damping profile of the PML (see the module comment of the oracle step):
+// d(s) = d0 (s/L)^npower, d0 = (npower+1) vpml ln(1/R0) / (2 L), s counted in
+// whole cells from the interface (first PML cell s = h), L = npml*h.
+void damping(const fdfk_params& p, std::vector<DampCol>& dx, std::vector<DampCol>& dz)
+{
+    const int NX = p.nx + 2 * p.npml, NZ = p.nz + p.npml;
+    const double lg = std::log(1.0 / p.R0);
+    const double Lx = (double)p.npml * p.dx, Lz = (double)p.npml * p.dz;
+    const double d0x = (p.npower + 1) * (double)p.vpml * lg / (2.0 * Lx);
+    const double d0z = (p.npower + 1) * (double)p.vpml * lg / (2.0 * Lz);
+    dx.assign(NX, DampCol{0.f, 0.f});
+    dz.assign(NZ, DampCol{0.f, 0.f});
+    for (int c = 0; c < NX; ++c) {
+        int ix = c + 1 - p.npml;
+        double s = 0.0, sg = 0.0;
+        if (ix <= 0) { s = (double)(1 - ix) * p.dx / Lx; sg = -1.0; }
+        else if (ix > p.nx) { s = (double)(ix - p.nx) * p.dx / Lx; sg = 1.0; }
+        else continue;
+        double d = d0x * std::pow(s, p.npower), dp = p.npower * d0x * std::pow(s, p.npower - 1) / Lx;
+        dx[c] = DampCol{(float)(d * p.dt), (float)(sg * dp * p.dt)};
+    }
+    for (int r = 0; r < NZ; ++r) {
+        int iz = r + 1;
+        if (iz <= p.nz) continue;
+        double s = (double)(iz - p.nz) * p.dz / Lz;
+        double d = d0z * std::pow(s, p.npower), dp = p.npower * d0z * std::pow(s, p.npower - 1) / Lz;
+        dz[r] = DampCol{(float)(d * p.dt), (float)(dp * p.dt)};
+    }
+}
+
+int zero_state(fdfk_session* s)
+{
+    const size_t n = (size_t)s->ldz * s->NX;
+    for (int l = 0; l < 2; ++l) {
+        CK(cudaMemsetAsync(s->ux[l], 0, n * sizeof(float), s->stream));
+        CK(cudaMemsetAsync(s->uz[l], 0, n * sizeof(float), s->stream));
+    }
+    for (int k = 0; k < 24; ++k)
+        for (int l = 0; l < 2; ++l)
+            if (s->bu[k][l]) CK(cudaMemsetAsync(s->bu[k][l], 0, bu_elems(s->p, k) * sizeof(float), s->stream));
+    for (int k = 0; k < 12; ++k)
+        if (s->bp[k]) CK(cudaMemsetAsync(s->bp[k], 0, bp_elems(s->p, k) * sizeof(float), s->stream));
+    s->cur = 0;
+    s->it = 0;
+    s->isis = 0;
+    s->istp = 0;
+    return FDFK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdfk_version(void) { return 100; }
+
+const char* fdfk_last_error(void) { return g_err.c_str(); }
+
+long long fdfk_kernel_launches(void) { return g_launches.load(); }
+
+int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out)
+{
+    if (!out) return fail(FDFK_EINVAL, "out is NULL");
+    *out = nullptr;
+    int rc = validate(p);
+    if (rc) return rc;
+    if (!c) return fail(FDFK_EINVAL, "c is NULL");
+    fdfk_session* s = new (std::nothrow) fdfk_session();
+    if (!s) return fail(FDFK_ENOMEM, "host allocation failed");
+    s->p = *p;
+    s->NZ = p->nz + p->npml;
+    s->NX = p->nx + 2 * p->npml;
+    s->ldz = (s->NZ + 31) / 32 * 32;
+    const size_t n = (size_t)s->ldz * s->NX;
+
+    auto alloc = [&](void** ptr, size_t bytes) -> int {
+        if (bytes == 0) { *ptr = nullptr; return FDFK_OK; }
+        cudaError_t e = cudaMalloc(ptr, bytes);
+        if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? FDFK_ENOMEM : FDFK_ECUDA,
+                                          std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        return FDFK_OK;
+    };
+#define AL(ptr, bytes) do { int r_ = alloc((void**)&(ptr), (bytes)); if (r_) { free_session(s); return r_; } } while (0)
+    AL(s->kdt2, n * sizeof(float));
+    AL(s->lam, n * sizeof(float));
+    AL(s->mu, n * sizeof(float));
+    for (int l = 0; l < 2; ++l) { AL(s->ux[l], n * sizeof(float)); AL(s->uz[l], n * sizeof(float)); }
+    for (int k = 0; k < 18; ++k)          // l, r, b (the top PML is not used with a free surface)
+        for (int l = 0; l < 2; ++l) AL(s->bu[k][l], bu_elems(*p, k) * sizeof(float));
+    for (int k = 0; k < 12; ++k)
+        if (k < 4 || k >= 8) AL(s->bp[k], bp_elems(*p, k) * sizeof(float));
+    AL(s->dampx, s->NX * sizeof(DampCol));
+    AL(s->dampz, s->NZ * sizeof(DampCol));
+    for (int k = 0; k < NSTRIP; ++k) AL(s->strip[k], strip_elems(*p, k) * (size_t)(p->nt + 1) * sizeof(float));
+#undef AL
+    s->have_bg.assign(p->nt + 1, 0);
+
+    float stag[kMaxOrder + 1][kMaxOrder + 1], coll[kMaxOrder + 1][kMaxOrder + 1];
+    fd_tables(stag, coll);
+    cudaError_t e = set_coefficients(&stag[0][0], &coll[0][0]);
+    if (e != cudaSuccess) { free_session(s); return fail(FDFK_ECUDA, std::string("coefficients: ") + cudaGetErrorString(e)); }
+
+    std::vector<DampCol> dx, dz;
+    damping(*p, dx, dz);
+    if ((rc = upload_material(s, c)) != FDFK_OK) { free_session(s); return rc; }
+    if (cudaMemcpy(s->dampx, dx.data(), dx.size() * sizeof(DampCol), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(s->dampz, dz.data(), dz.size() * sizeof(DampCol), cudaMemcpyHostToDevice) != cudaSuccess) {
+        free_session(s);
+        return fail(FDFK_ECUDA, "damping upload failed");
+    }
+    if ((rc = zero_state(s)) != FDFK_OK) { free_session(s); return rc; }
+
+    StepArgs& a = s->base;
+    a.nx = p->nx; a.nz = p->nz; a.npml = p->npml; a.norder = p->norder; a.nbd = p->nbd;
+    a.NZ = s->NZ; a.NX = s->NX; a.ldz = s->ldz;
+    a.dx = p->dx; a.dz = p->dz;
+    a.dx2r = (float)(1.0 / (double)(p->dx * p->dx));
+    a.dx2p = 1.0f / (p->dx * p->dx);
+    a.dz2 = 1.0f / (p->dz * p->dz);
+    a.dt = (float)p->dt;
+    a.kdt2 = s->kdt2; a.lam = s->lam; a.mu = s->mu;
+    a.dampx = s->dampx; a.dampz = s->dampz;
+    for (int k = 0; k < NSTRIP; ++k) a.strip[k] = s->strip[k];
+    a.tiles_int_z = (p->nz + kTZ - 1) / kTZ;
+    a.tiles_int_x = (p->nx + kTX - 1) / kTX;
+    a.tiles_l_z = (p->nz + kTZ - 1) / kTZ;
+    a.tiles_l_x = (p->npml + kTX - 1) / kTX;
+    a.tiles_b_z = (p->npml + kTZ - 1) / kTZ;
+    a.tiles_b_x = (s->NX + kTX - 1) / kTX;
+    a.n_tiles = a.tiles_int_z * a.tiles_int_x + 2 * a.tiles_l_z * a.tiles_l_x + a.tiles_b_z * a.tiles_b_x;
+    *out = s;
+    return FDFK_OK;
+}
+
+int fdfk_session_set_stream(fdfk_session* s, void* stream)
+{
+    if (!s) return fail(FDFK_EINVAL, "session is NULL");
+    s->stream = (cudaStream_t)stream;
+    return FDFK_OK;
+}
+
+int fdfk_session_upload_background(fdfk_session* s, const float* const strips[12], int t0, int count)
+{
+    if (!s || !strips) return fail(FDFK_EINVAL, "NULL argument");
+    if (t0 < 0 || count < 0 || t0 + count > s->p.nt + 1) return fail(FDFK_EINVAL, "time range outside 0..nt");
+    for (int k = 0; k < NSTRIP; ++k) {
+        if (!strips[k]) return fail(FDFK_EINVAL, "strip array is NULL");
+        const size_t per = strip_elems(s->p, k);
+        CK(cudaMemcpyAsync(s->strip[k] + per * t0, strips[k] + per * t0, per * (size_t)count * sizeof(float),
+                           cudaMemcpyHostToDevice, s->stream));
+    }
+    for (int t = t0; t < t0 + count; ++t) s->have_bg[t] = 1;
+    return FDFK_OK;
+}
+
+int fdfk_session_set_receivers(fdfk_session* s, int nrcv, const float* rx, const float* rz, float x0, float z0,
+                               int nstp, int nsis)
+{
+    if (!s) return fail(FDFK_EINVAL, "session is NULL");
+    if (nrcv < 0 || (nrcv > 0 && (!rx || !rz)) || nstp < 1 || nsis < 0) return fail(FDFK_EINVAL, "bad receiver arguments");
+    const float xmax = x0 + (s->p.nx - 1) * s->p.dx, zmax = z0 + (s->p.nz - 1) * s->p.dz;
+    for (int r = 0; r < nrcv; ++r)
+        if (rx[r] < x0 || rx[r] > xmax || rz[r] < z0 || rz[r] > zmax)
+            return fail(FDFK_EINVAL, "receiver " + std::to_string(r + 1) + " lies outside the model");
+    cudaFree(s->rx); cudaFree(s->rz); cudaFree(s->seisx); cudaFree(s->seisz);
+    s->rx = s->rz = s->seisx = s->seisz = nullptr;
+    s->nrcv = nrcv; s->nstp = nstp; s->nsis = nsis; s->x0 = x0; s->z0 = z0;
+    if (nrcv > 0) {
+        const size_t ns = (size_t)(nsis + 1) * nrcv;
+        CK(cudaMalloc((void**)&s->rx, nrcv * sizeof(float)));
+        CK(cudaMalloc((void**)&s->rz, nrcv * sizeof(float)));
+        CK(cudaMalloc((void**)&s->seisx, ns * sizeof(float)));
+        CK(cudaMalloc((void**)&s->seisz, ns * sizeof(float)));
+        CK(cudaMemcpyAsync(s->rx, rx, nrcv * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->rz, rz, nrcv * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemsetAsync(s->seisx, 0, ns * sizeof(float), s->stream));
+        CK(cudaMemsetAsync(s->seisz, 0, ns * sizeof(float), s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    // the sampling clock restarts with the loop (src/FDFK2D.f90:315-316)
+    s->isis = s->istp * nstp;
+    return FDFK_OK;
+}
+
+int fdfk_session_advance(fdfk_session* s, int nsteps)
+{
+    if (!s) return fail(FDFK_EINVAL, "session is NULL");
+    if (nsteps < 0) return fail(FDFK_EINVAL, "nsteps must be >= 0");
+    if (s->it + nsteps > s->p.nt + 1) return fail(FDFK_EINVAL, "advance past the last time index nt");
+    for (int k = 0; k < nsteps; ++k) {
+        const int it = s->it;
+        if (!s->have_bg[it]) return fail(FDFK_ESTATE, "no background uploaded for time index " + std::to_string(it));
+        StepArgs a = s->base;
+        for (int l = 0; l < 2; ++l) { a.ux[l] = s->ux[l]; a.uz[l] = s->uz[l]; }
+        for (int q = 0; q < 24; ++q) for (int l = 0; l < 2; ++l) a.bu[q][l] = s->bu[q][l];
+        for (int q = 0; q < 12; ++q) a.bp[q] = s->bp[q];
+        a.it = it;
+        a.cur = s->cur;
+        a.nrcv = 0;
+        if (s->nrcv > 0 && s->isis == it && s->istp <= s->nsis) {
+            a.nrcv = s->nrcv;
+            a.sample_index = s->istp;
+            a.nsamp = s->nsis + 1;
+            a.x0 = s->x0; a.z0 = s->z0;
+            a.rx = s->rx; a.rz = s->rz;
+            a.seisx = s->seisx; a.seisz = s->seisz;
+            s->istp += 1;
+            s->isis += s->nstp;
+        }
+        cudaError_t e = launch_step(a, s->stream);
+        if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("step launch: ") + cudaGetErrorString(e));
+        g_launches.fetch_add(1);
+        s->cur ^= 1;
+        s->it += 1;
+    }
+    return FDFK_OK;
+}
+
+int fdfk_session_step_index(const fdfk_session* s) { return s ? s->it : FDFK_EINVAL; }
+
+int fdfk_session_synchronize(fdfk_session* s)
+{
+    if (!s) return fail(FDFK_EINVAL, "session is NULL");
+    CK(cudaStreamSynchronize(s->stream));
+    return FDFK_OK;
+}
+
+int fdfk_session_download_seismograms(fdfk_session* s, float* seisx, float* seisz)
+{
+    if (!s || !seisx || !seisz) return fail(FDFK_EINVAL, "NULL argument");
+    if (s->nrcv == 0) return FDFK_OK;
+    const size_t ns = (size_t)(s->nsis + 1) * s->nrcv;
+    CK(cudaMemcpyAsync(seisx, s->seisx, ns * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(seisz, s->seisz, ns * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FDFK_OK;
+}
+
+int fdfk_session_download_seismogram_range(fdfk_session* s, int first, int count, float* seisx, float* seisz)
+{
+    if (!s || !seisx || !seisz) return fail(FDFK_EINVAL, "NULL argument");
+    if (first < 0 || count < 0 || first + count > s->nsis + 1) return fail(FDFK_EINVAL, "sample range outside 0..nsis");
+    if (s->nrcv == 0 || count == 0) return FDFK_OK;
+    const size_t pitch = (size_t)(s->nsis + 1) * sizeof(float);
+    CK(cudaMemcpy2DAsync(seisx, count * sizeof(float), s->seisx + first, pitch, count * sizeof(float), s->nrcv,
+                         cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpy2DAsync(seisz, count * sizeof(float), s->seisz + first, pitch, count * sizeof(float), s->nrcv,
+                         cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FDFK_OK;
+}
+
+int fdfk_session_upload_state(fdfk_session* s, const float* ux, const float* uz, const float* const bp[12],
+                              const float* const bu[24], int it)
+{
+    if (!s || !ux || !uz || !bp || !bu) return fail(FDFK_EINVAL, "NULL argument");
+    if (it < 0 || it > s->p.nt + 1) return fail(FDFK_EINVAL, "it outside 0..nt+1");
+    const size_t n = (size_t)s->ldz * s->NX;
+    std::vector<float> lv[4];
+    for (auto& v : lv) v.assign(n, 0.f);
+    for (int x = 0; x < s->NX; ++x)
+        for (int z = 0; z < s->NZ; ++z) {
+            size_t src = 2 * ((size_t)z + (size_t)s->NZ * x), dst = (size_t)z + (size_t)s->ldz * x;
+            lv[0][dst] = ux[src]; lv[1][dst] = ux[src + 1];
+            lv[2][dst] = uz[src]; lv[3][dst] = uz[src + 1];
+        }
+    s->cur = 0;
+    CK(cudaMemcpyAsync(s->ux[0], lv[0].data(), n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->ux[1], lv[1].data(), n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->uz[0], lv[2].data(), n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->uz[1], lv[3].data(), n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    for (int k = 0; k < 12; ++k) {
+        if (!s->bp[k]) continue;
+        if (!bp[k]) return fail(FDFK_EINVAL, "bp array is NULL");
+        CK(cudaMemcpyAsync(s->bp[k], bp[k], bp_elems(s->p, k) * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    }
+    std::vector<float> pl[2];
+    for (int k = 0; k < 24; ++k) {
+        if (!s->bu[k][0]) continue;
+        if (!bu[k]) return fail(FDFK_EINVAL, "bu array is NULL");
+        const size_t m = bu_elems(s->p, k);
+        pl[0].resize(m); pl[1].resize(m);
+        for (size_t i = 0; i < m; ++i) { pl[0][i] = bu[k][2 * i]; pl[1][i] = bu[k][2 * i + 1]; }
+        CK(cudaMemcpyAsync(s->bu[k][0], pl[0].data(), m * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->bu[k][1], pl[1].data(), m * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    s->it = it;
+    s->istp = 0;
+    s->isis = 0;
+    return FDFK_OK;
+}
+
+int fdfk_session_download_state(fdfk_session* s, float* ux, float* uz, float* const bp[12], float* const bu[24])
+{
+    if (!s || !ux || !uz || !bp || !bu) return fail(FDFK_EINVAL, "NULL argument");
+    const size_t n = (size_t)s->ldz * s->NX;
+    std::vector<float> lv[4];
+    for (auto& v : lv) v.resize(n);
+    const int c = s->cur, o = c ^ 1;
+    CK(cudaMemcpyAsync(lv[0].data(), s->ux[c], n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(lv[1].data(), s->ux[o], n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(lv[2].data(), s->uz[c], n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(lv[3].data(), s->uz[o], n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    const int npml = s->p.npml, nx = s->p.nx;
+    for (int x = 0; x < s->NX; ++x)
+        for (int z = 0; z < s->NZ; ++z) {
+            size_t dst = 2 * ((size_t)z + (size_t)s->NZ * x), src = (size_t)z + (size_t)s->ldz * x;
+            const int ix = x + 1 - npml, iz = z + 1;
+            // the outer frame is never advanced: its level 2 is left as the caller holds it
+            const bool frame = ix == 1 - npml || ix == nx + npml || iz == s->NZ;
+            ux[dst] = lv[0][src];
+            uz[dst] = lv[2][src];
+            if (!frame) { ux[dst + 1] = lv[1][src]; uz[dst + 1] = lv[3][src]; }
+        }
+    for (int k = 0; k < 12; ++k) {
+        if (!s->bp[k]) continue;
+        if (!bp[k]) return fail(FDFK_EINVAL, "bp array is NULL");
+        CK(cudaMemcpyAsync(bp[k], s->bp[k], bp_elems(s->p, k) * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    }
+    std::vector<float> pl[2];
+    for (int k = 0; k < 24; ++k) {
+        if (!s->bu[k][0]) continue;
+        if (!bu[k]) return fail(FDFK_EINVAL, "bu array is NULL");
+        const size_t m = bu_elems(s->p, k);
+        pl[0].resize(m); pl[1].resize(m);
+        CK(cudaMemcpyAsync(pl[0].data(), s->bu[k][c], m * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaMemcpyAsync(pl[1].data(), s->bu[k][o], m * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        // cells on the outer frame are never advanced: both levels stay as the caller holds them
+        const bool sidearr = k < 12;
+        const int n1 = sidearr ? s->p.nz : npml, n2 = sidearr ? npml : s->NX;
+        for (int j = 0; j < n2; ++j)
+            for (int r = 0; r < n1; ++r) {
+                bool frame;
+                if (sidearr) frame = (k < 6) ? j == 0 : j == npml - 1;
+                else frame = r == npml - 1 || j == 0 || j == s->NX - 1;
+                if (frame) continue;
+                const size_t i = (size_t)r + (size_t)n1 * j;
+                bu[k][2 * i] = pl[0][i];
+                bu[k][2 * i + 1] = pl[1][i];
+            }
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return FDFK_OK;
+}
+
+void fdfk_session_destroy(fdfk_session* s)
+{
+    if (s && s->stream) cudaStreamSynchronize(s->stream);
+    free_session(s);
+}
+
+int fdfk_simulate(const fdfk_params* p, const float* c, const float* const strips[12], int nrcv, const float* rx,
+                  const float* rz, float x0, float z0, int nstp, int nsis, float* seisx, float* seisz)
+{
+    fdfk_session* s = nullptr;
+    int rc = fdfk_session_create(p, c, &s);
+    if (rc) return rc;
+    if ((rc = fdfk_session_upload_background(s, strips, 0, p->nt + 1)) ||
+        (rc = fdfk_session_set_receivers(s, nrcv, rx, rz, x0, z0, nstp, nsis)) ||
+        (rc = fdfk_session_advance(s, p->nt + 1)) ||
+        (rc = fdfk_session_download_seismograms(s, seisx, seisz))) {
+        fdfk_session_destroy(s);
+        return rc;
+    }
+    fdfk_session_destroy(s);
+    return FDFK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// gfortran-ABI drop-in
+// ---------------------------------------------------------------------------
+static fdfk_session* g_legacy = nullptr;
+
+void updatedispl_(const int* norder, const int* nx, const int* nz, const int* npml, const int* izt,
+                  const int* is_PML_top, const int* npower, const int* nbd, const int* it, const int* nt,
+                  const float* dx, const float* dz, const double* dt, const float* vpml, const double* R0,
+                  const float* uxl_reg, const float* uzl_reg, const float* uxr_reg, const float* uzr_reg,
+                  const float* uxb_reg, const float* uzb_reg, const float* uxl_pml, const float* uzl_pml,
+                  const float* uxr_pml, const float* uzr_pml, const float* uxb_pml, const float* uzb_pml,
+                  const float* c, const double* coef0, const double* coef1, float* ux, float* uz,
+                  float* bpxlx, float* bpzlx, float* bpxrx, float* bpzrx, float* bpxtx, float* bpxtz, float* bpztx,
+                  float* bpztz, float* bpxbx, float* bpxbz, float* bpzbx, float* bpzbz,
+                  float* bux1l, float* bux2l, float* bux3l, float* buz1l, float* buz2l, float* buz3l,
+                  float* bux1r, float* bux2r, float* bux3r, float* buz1r, float* buz2r, float* buz3r,
+                  float* bux1b, float* bux2b, float* bux3b, float* buz1b, float* buz2b, float* buz3b,
+                  float* bux1t, float* bux2t, float* bux3t, float* buz1t, float* buz2t, float* buz3t)
+{
+    (void)coef0; (void)coef1;  // the weights are regenerated from their closed form
+    fdfk_params p{};
+    p.norder = *norder; p.nx = *nx; p.nz = *nz; p.npml = *npml; p.is_PML_top = *is_PML_top ? 1 : 0;
+    p.npower = *npower; p.nbd = *nbd; p.nt = 0; p.dx = *dx; p.dz = *dz; p.dt = *dt; p.vpml = *vpml; p.R0 = *R0;
+    auto die = [](const char* what) {
+        std::fprintf(stderr, "fdfk_gb300 updatedispl_: %s (%s)\n", what, g_err.c_str());
+        std::abort();
+    };
+    if (*izt != 1 || p.is_PML_top) { g_err = "is_PML_top"; die("only the free-surface top boundary is implemented"); }
+    const bool same = g_legacy && std::memcmp(&g_legacy->p, &p, sizeof(p)) == 0;
+    if (!same) {
+        fdfk_session_destroy(g_legacy);
+        g_legacy = nullptr;
+        if (fdfk_session_create(&p, c, &g_legacy)) die("session create failed");
+    } else if (upload_material(g_legacy, c)) {
+        die("material upload failed");
+    }
+    // the strips of this call, time index *it, uploaded as time 0 of a one-sample session
+    const float* all[12] = {uxl_reg, uzl_reg, uxr_reg, uzr_reg, uxb_reg, uzb_reg,
+                            uxl_pml, uzl_pml, uxr_pml, uzr_pml, uxb_pml, uzb_pml};
+    const float* at[12];
+    for (int k = 0; k < 12; ++k) at[k] = all[k] + strip_elems(p, k) * (size_t)(*it);
+    (void)nt;
+    float* bp[12] = {bpxlx, bpzlx, bpxrx, bpzrx, bpxtx, bpxtz, bpztx, bpztz, bpxbx, bpxbz, bpzbx, bpzbz};
+    float* bu[24] = {bux1l, bux2l, bux3l, buz1l, buz2l, buz3l, bux1r, bux2r, bux3r, buz1r, buz2r, buz3r,
+                     bux1b, bux2b, bux3b, buz1b, buz2b, buz3b, bux1t, bux2t, bux3t, buz1t, buz2t, buz3t};
+    if (fdfk_session_upload_background(g_legacy, at, 0, 1) ||
+        fdfk_session_upload_state(g_legacy, ux, uz, bp, bu, 0) ||
+        fdfk_session_advance(g_legacy, 1) ||
+        fdfk_session_download_state(g_legacy, ux, uz, bp, bu))
+        die("step failed");
+}
+
+}  // extern "C"

@@ -1,0 +1,630 @@
+// Fused hybrid FD-FK time step for sm_103a.  See fdfk_sweep.cuh.
+//
+// Operator semantics follow FDFK2D src/Submain.f90:
+//   dxx(M u)  diffx2_* (:764-937)  staggered derivative of H(M) * staggered derivative
+//   dzz(M u)  diffz2_* (:939-1109)
+//   dzx(M u)  diffzx_* (:251-507)  collocated d/dx of M * collocated d/dz u
+//   dxz(M u)  diffxz_* (:509-762)  collocated d/dz of M * collocated d/dx u
+// with edge-reduced orders norder(ix) = min(ix+npml-1, nx+npml-ix, norder),
+// norder(iz) = min(iz-izt, nz+npml-iz, norder).  H is the harmonic mean
+// 2/(1/M_a + 1/M_b), formed with IEEE divisions as the reference forms it.
+//
+// The staggered products G = H * D_stag(u) are formed once per half point in
+// shared memory and reused by the 2*norder output cells that read them; the
+// reference recomputes them per output cell.  At a half point between cells a
+// and a+1 the reference uses order(a) when the point lies right of the output
+// cell and order(a+1) when it lies left of it; the two differ only within
+// norder cells of the outer frame, where the second variant is recomputed.
+#include "fdfk_sweep.cuh"
+
+#include <cuda_runtime.h>
+
+namespace fdfk {
+
+__constant__ float c_stag[kMaxOrder + 1][kMaxOrder + 1];  // [n][j]: fd_coef0(j, n), zero for j > n
+__constant__ float c_coll[kMaxOrder + 1][kMaxOrder + 1];  // [n][j]: fd_coef1(j, n)
+
+template <int NO>
+struct Tile {
+    static constexpr int H = 2 * NO - 1;          // reach of dxx / dzz
+    static constexpr int UZ = kTZ + 2 * H;        // u tile (z fastest)
+    static constexpr int UX = kTX + 2 * H;
+    static constexpr int MZ = kTZ + 2 * NO;       // material tile
+    static constexpr int MX = kTX + 2 * NO;
+    static constexpr int XW = kTX + 2 * NO;       // x extent of x-consumed arrays
+    static constexpr int ZW = kTZ + 2 * NO;       // z extent of z-consumed arrays
+    static constexpr int U = UZ * UX;
+    static constexpr int M = MZ * MX;
+    static constexpr int AX = kTZ * XW;
+    static constexpr int AZ = ZW * kTX;
+    static constexpr int total = 2 * U + 5 * M + 4 * AX + 4 * AZ;
+};
+
+struct Rect {
+    int side;       // 0 interior, 1 left PML, 2 right PML, 3 bottom PML
+    int z0, x0;     // first row / column of the tile
+    int zlo, zhi, xlo, xhi;  // output rectangle (inclusive)
+};
+
+__device__ __forceinline__ int ordx(const StepArgs& a, int ix, int NO)
+{
+    int n = min(min(ix + a.npml - 1, a.nx + a.npml - ix), NO);
+    return n < 0 ? 0 : n;
+}
+__device__ __forceinline__ int ordz(const StepArgs& a, int iz, int NO)
+{
+    int n = min(min(iz - 1, a.nz + a.npml - iz), NO);
+    return n < 0 ? 0 : n;
+}
+__device__ __forceinline__ size_t gidx(const StepArgs& a, int iz, int ix)
+{
+    return (size_t)(iz - 1) + (size_t)(ix + a.npml - 1) * (size_t)a.ldz;
+}
+
+// Background value at (iz, ix) on the outer strips (Omega_II), or 0.
+__device__ __forceinline__ void outer_bg(const StepArgs& a, int iz, int ix, float& bx, float& bz)
+{
+    const int nx = a.nx, nz = a.nz, nbd = a.nbd, it = a.it;
+    bx = 0.f; bz = 0.f;
+    if (iz >= 1 && iz <= nz) {
+        if (ix >= 1 - nbd && ix <= 0) {
+            size_t o = (size_t)(iz - 1) + (size_t)nz * ((size_t)(ix - (1 - nbd)) + (size_t)nbd * it);
+            bx = __ldg(a.strip[UXL_PML] + o); bz = __ldg(a.strip[UZL_PML] + o);
+        } else if (ix >= nx + 1 && ix <= nx + nbd) {
+            size_t o = (size_t)(iz - 1) + (size_t)nz * ((size_t)(ix - nx - 1) + (size_t)nbd * it);
+            bx = __ldg(a.strip[UXR_PML] + o); bz = __ldg(a.strip[UZR_PML] + o);
+        }
+    } else if (iz >= nz + 1 && iz <= nz + nbd && ix >= 1 - nbd && ix <= nx + nbd) {
+        size_t o = (size_t)(iz - nz - 1) + (size_t)nbd * ((size_t)(ix - (1 - nbd)) + (size_t)(nx + 2 * nbd) * it);
+        bx = __ldg(a.strip[UXB_PML] + o); bz = __ldg(a.strip[UZB_PML] + o);
+    }
+}
+
+// Background value at (iz, ix) on the inner strips (Omega_I), or 0.
+__device__ __forceinline__ void inner_bg(const StepArgs& a, int iz, int ix, float& bx, float& bz)
+{
+    const int nx = a.nx, nz = a.nz, nbd = a.nbd, it = a.it;
+    bx = 0.f; bz = 0.f;
+    if (ix < 1 || ix > nx || iz < 1 || iz > nz) return;
+    if (iz <= nz - nbd) {
+        if (ix <= nbd) {
+            size_t o = (size_t)(iz - 1) + (size_t)(nz - nbd) * ((size_t)(ix - 1) + (size_t)nbd * it);
+            bx = __ldg(a.strip[UXL_REG] + o); bz = __ldg(a.strip[UZL_REG] + o);
+        } else if (ix >= nx - nbd + 1) {
+            size_t o = (size_t)(iz - 1) + (size_t)(nz - nbd) * ((size_t)(ix - (nx - nbd + 1)) + (size_t)nbd * it);
+            bx = __ldg(a.strip[UXR_REG] + o); bz = __ldg(a.strip[UZR_REG] + o);
+        }
+    } else {
+        size_t o = (size_t)(iz - (nz - nbd + 1)) + (size_t)nbd * ((size_t)(ix - 1) + (size_t)nx * it);
+        bx = __ldg(a.strip[UXB_REG] + o); bz = __ldg(a.strip[UZB_REG] + o);
+    }
+}
+
+__device__ __forceinline__ Rect decode_tile(const StepArgs& a, int b)
+{
+    Rect r;
+    int ni = a.tiles_int_z * a.tiles_int_x;
+    int nl = a.tiles_l_z * a.tiles_l_x;
+    if (b < ni) {
+        r.side = 0;
+        r.z0 = 1 + (b % a.tiles_int_z) * kTZ; r.x0 = 1 + (b / a.tiles_int_z) * kTX;
+        r.zlo = 1; r.zhi = a.nz; r.xlo = 1; r.xhi = a.nx;
+        return r;
+    }
+    b -= ni;
+    if (b < 2 * nl) {
+        int right = b >= nl;
+        if (right) b -= nl;
+        r.side = right ? 2 : 1;
+        r.zlo = 1; r.zhi = a.nz;
+        r.xlo = right ? a.nx + 1 : 1 - a.npml;
+        r.xhi = right ? a.nx + a.npml : 0;
+        r.z0 = 1 + (b % a.tiles_l_z) * kTZ; r.x0 = r.xlo + (b / a.tiles_l_z) * kTX;
+        return r;
+    }
+    b -= 2 * nl;
+    r.side = 3;
+    r.zlo = a.nz + 1; r.zhi = a.nz + a.npml; r.xlo = 1 - a.npml; r.xhi = a.nx + a.npml;
+    r.z0 = r.zlo + (b % a.tiles_b_z) * kTZ; r.x0 = r.xlo + (b / a.tiles_b_z) * kTX;
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Receiver sampling (loadseis, src/Submain.f90:33-116), FP64 weights and sum.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double delta_weight(double x)
+{
+    double x2 = x * x, x3 = x2 * x;
+    if (x <= 1.0) return 1.0 + x2 * (-5.0 / 4.0 + x2 * (21.0 / 4.0)) + x3 * (-35.0 / 12.0 + x2 * (-25.0 / 12.0));
+    if (x <= 2.0)
+        return -4.0 + (75.0 / 4.0) * x + x2 * (-245.0 / 8.0 + x2 * (-63.0 / 8.0)) + x3 * (545.0 / 24.0 + x2 * (25.0 / 24.0));
+    if (x <= 3.0)
+        return 18.0 + (-153.0 / 4.0) * x + x2 * (255.0 / 8.0 + x2 * (21.0 / 8.0)) + x3 * (-313.0 / 24.0 + x2 * (-5.0 / 24.0));
+    return 0.0;
+}
+
+__device__ void sample_receivers(const StepArgs& a, int blk)
+{
+    int r = blk * kThreads + threadIdx.x;
+    if (r >= a.nrcv) return;
+    const float* ux = a.ux[a.cur];
+    const float* uz = a.uz[a.cur];
+    float rx = a.rx[r], rz = a.rz[r];
+    int irx = (int)floorf((rx - a.x0) / a.dx) + 1;
+    int irz = (int)floorf((rz - a.z0) / a.dz) + 1;
+    double sx = 0.0, sz = 0.0;
+    for (int ix = max(1 - a.npml, irx - 3); ix <= min(a.nx + a.npml, irx + 3); ++ix) {
+        double x = fabs((double)__fadd_rn(a.x0, __fmul_rn((float)(ix - 1), a.dx)) - (double)rx) / (double)a.dx;
+        double bx = delta_weight(x);
+        for (int iz = max(1, irz - 3); iz <= min(a.nz + a.npml, irz + 3); ++iz) {
+            double z = fabs((double)__fadd_rn(a.z0, __fmul_rn((float)(iz - 1), a.dz)) - (double)rz) / (double)a.dz;
+            double w = bx * delta_weight(z);
+            size_t g = gidx(a, iz, ix);
+            sx += w * (double)ux[g];
+            sz += w * (double)uz[g];
+        }
+    }
+    size_t o = (size_t)a.sample_index + (size_t)a.nsamp * (size_t)r;
+    a.seisx[o] = (float)sx;
+    a.seisz[o] = (float)sz;
+}
+
+// ---------------------------------------------------------------------------
+// The step kernel.
+// ---------------------------------------------------------------------------
+template <int NO>
+__global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
+{
+    using T = Tile<NO>;
+    constexpr int H = T::H;
+    extern __shared__ float sm[];
+    if ((int)blockIdx.x >= a.n_tiles) {
+        sample_receivers(a, blockIdx.x - a.n_tiles);
+        return;
+    }
+    const Rect R = decode_tile(a, blockIdx.x);
+    const bool pml = R.side != 0;
+    const int tid = threadIdx.x;
+    const int nx = a.nx, nz = a.nz, npml = a.npml;
+    const int NZ = a.NZ;
+
+    float* sux = sm;
+    float* suz = sux + T::U;
+    float* sLam = suz + T::U;
+    float* sMu = sLam + T::M;
+    float* sL2m = sMu + T::M;
+    float* sRL2m = sL2m + T::M;
+    float* sRMu = sRL2m + T::M;
+    float* gxA = sRMu + T::M;   // H(l2m) * Dstag_x(ux)   [label][z]
+    float* gxB = gxA + T::AX;   // H(mu)  * Dstag_x(uz)
+    float* v1 = gxB + T::AX;    // lam * Dz(uz)/dz        [x][z]  (dzx(lam uz))
+    float* v4 = v1 + T::AX;     // mu  * Dz(ux)/dz                 (dzx(mu ux))
+    float* gzA = v4 + T::AX;    // H(l2m) * Dstag_z(uz)   [x][label]
+    float* gzB = gzA + T::AZ;   // H(mu)  * Dstag_z(ux)
+    float* v2 = gzB + T::AZ;    // mu  * Dx(uz)/dx        [x][z]  (dxz(mu uz))
+    float* v3 = v2 + T::AZ;     // lam * Dx(ux)/dx                 (dxz(lam ux))
+
+    const float* uxc = a.ux[a.cur];
+    const float* uzc = a.uz[a.cur];
+
+    // ---- phase 0: field tile (with injection) and material tile -------------
+    for (int i = tid; i < T::U; i += kThreads) {
+        int sz = i % T::UZ, sx = i / T::UZ;
+        int iz = R.z0 - H + sz, ix = R.x0 - H + sx;
+        float vx = 0.f, vz = 0.f;
+        if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
+            size_t g = gidx(a, iz, ix);
+            vx = uxc[g];
+            vz = uzc[g];
+            float bx, bz;
+            if (!pml) {
+                outer_bg(a, iz, ix, bx, bz);
+                vx += bx; vz += bz;
+            } else {
+                inner_bg(a, iz, ix, bx, bz);
+                vx -= bx; vz -= bz;
+            }
+        }
+        sux[i] = vx;
+        suz[i] = vz;
+    }
+    for (int i = tid; i < T::M; i += kThreads) {
+        int mz = i % T::MZ, mx = i / T::MZ;
+        int iz = R.z0 - NO + mz, ix = R.x0 - NO + mx;
+        float l = 0.f, m = 1.f;
+        if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
+            size_t g = gidx(a, iz, ix);
+            l = __ldg(a.lam + g);
+            m = __ldg(a.mu + g);
+        }
+        float l2 = l + 2.0f * m;
+        sLam[i] = l;
+        sMu[i] = m;
+        sL2m[i] = l2;
+        sRL2m[i] = 1.0f / l2;
+        sRMu[i] = 1.0f / m;
+    }
+    __syncthreads();
+
+#define SU(arr, z, x) arr[((x) + H) * T::UZ + ((z) + H)]
+#define SM(arr, z, x) arr[((x) + NO) * T::MZ + ((z) + NO)]
+
+    // ---- phase 1a: x-direction staggered products and dzx operands -----------
+    for (int i = tid; i < T::AX; i += kThreads) {
+        int z = i % kTZ, xl = i / kTZ;
+        int iz = R.z0 + z;
+        // staggered product at label L = xl - NO (half point between L and L+1)
+        if (xl < T::XW - 1) {
+            int L = xl - NO;
+            int n = ordx(a, R.x0 + L, NO);
+            float sx = 0.f, szv = 0.f;
+#pragma unroll
+            for (int j = 1; j <= NO; ++j) {
+                float c = c_stag[n][j];
+                sx = fmaf(c, SU(sux, z, L + j) - SU(sux, z, L + 1 - j), sx);
+                szv = fmaf(c, SU(suz, z, L + j) - SU(suz, z, L + 1 - j), szv);
+            }
+            float hl = 2.0f / (SM(sRL2m, z, L) + SM(sRL2m, z, L + 1));
+            float hm = 2.0f / (SM(sRMu, z, L) + SM(sRMu, z, L + 1));
+            gxA[i] = hl * sx;
+            gxB[i] = hm * szv;
+        }
+        // dzx operands at cell column x = xl - NO
+        {
+            int x = xl - NO;
+            int ix = R.x0 + x;
+            int n = ordz(a, iz, NO);
+            float dzz = 0.f, dzx = 0.f;
+#pragma unroll
+            for (int k = 1; k <= NO; ++k) {
+                float c = c_coll[n][k];
+                dzz = fmaf(c, SU(suz, z + k, x) - SU(suz, z - k, x), dzz);
+                dzx = fmaf(c, SU(sux, z + k, x) - SU(sux, z - k, x), dzx);
+            }
+            // diffzx_reg forms v on rows 2..nz; diffzx_pml on rows 2..NZ-1, columns 2-npml..nx+npml-1
+            bool valid = pml ? (iz >= 2 && iz <= NZ - 1 && ix >= 2 - npml && ix <= nx + npml - 1)
+                             : (iz >= 2 && iz <= nz && ix >= 1 - NO && ix <= nx + NO);
+            v1[i] = valid ? SM(sLam, z, x) * dzz / a.dz : 0.f;
+            v4[i] = valid ? SM(sMu, z, x) * dzx / a.dz : 0.f;
+        }
+    }
+    // ---- phase 1b: z-direction staggered products and dxz operands -----------
+    for (int i = tid; i < T::AZ; i += kThreads) {
+        int zl = i % T::ZW, x = i / T::ZW;
+        int ix = R.x0 + x;
+        if (zl < T::ZW - 1) {
+            int L = zl - NO;
+            int n = ordz(a, R.z0 + L, NO);
+            float sz_ = 0.f, sx = 0.f;
+#pragma unroll
+            for (int j = 1; j <= NO; ++j) {
+                float c = c_stag[n][j];
+                sz_ = fmaf(c, SU(suz, L + j, x) - SU(suz, L + 1 - j, x), sz_);
+                sx = fmaf(c, SU(sux, L + j, x) - SU(sux, L + 1 - j, x), sx);
+            }
+            float hl = 2.0f / (SM(sRL2m, L, x) + SM(sRL2m, L + 1, x));
+            float hm = 2.0f / (SM(sRMu, L, x) + SM(sRMu, L + 1, x));
+            gzA[i] = hl * sz_;
+            gzB[i] = hm * sx;
+        }
+        {
+            int z = zl - NO;
+            int iz = R.z0 + z;
+            int n = ordx(a, ix, NO);
+            float dxz = 0.f, dxx = 0.f;
+#pragma unroll
+            for (int k = 1; k <= NO; ++k) {
+                float c = c_coll[n][k];
+                dxz = fmaf(c, SU(suz, z, x + k) - SU(suz, z, x - k), dxz);
+                dxx = fmaf(c, SU(sux, z, x + k) - SU(sux, z, x - k), dxx);
+            }
+            // diffxz_reg forms v on rows 1..nz+norder, columns 1..nx; diffxz_pml on rows 1..NZ-1
+            bool valid = pml ? (iz >= 1 && iz <= NZ - 1 && ix >= 2 - npml && ix <= nx + npml - 1)
+                             : (iz >= 1 && iz <= nz + NO && ix >= 1 && ix <= nx);
+            v2[i] = valid ? SM(sMu, z, x) * dxz / a.dx : 0.f;
+            v3[i] = valid ? SM(sLam, z, x) * dxx / a.dx : 0.f;
+        }
+    }
+    __syncthreads();
+
+#define GXI(arr, z, L) arr[((L) + NO) * kTZ + (z)]
+#define VXI(arr, z, x) arr[((x) + NO) * kTZ + (z)]
+#define GZI(arr, L, x) arr[(x) * T::ZW + ((L) + NO)]
+#define VZI(arr, z, x) arr[(x) * T::ZW + ((z) + NO)]
+
+    // ---- phase 2: output cells ----------------------------------------------
+    const int z = tid % kTZ;
+    const int iz = R.z0 + z;
+    const float dx = a.dx, dz = a.dz;
+    const float dx2 = pml ? a.dx2p : a.dx2r;
+    for (int q = 0; q < kTX / (kThreads / kTZ); ++q) {
+        const int x = tid / kTZ + q * (kThreads / kTZ);
+        const int ix = R.x0 + x;
+        if (iz < R.zlo || iz > R.zhi || ix < R.xlo || ix > R.xhi) continue;
+        const size_t g = gidx(a, iz, ix);
+        const int nxo = ordx(a, ix, NO);
+        const int nzo = ordz(a, iz, NO);
+
+        if (pml && (ix == 1 - npml || ix == nx + npml || iz == NZ)) {
+            // outer frame: never advanced; keep level 1 across the plane swap
+            a.ux[a.cur ^ 1][g] = uxc[g];
+            a.uz[a.cur ^ 1][g] = uzc[g];
+            continue;
+        }
+
+        // x-direction second derivatives dxx(l2m ux), dxx(mu uz)
+        float x2a = 0.f, x2b = 0.f;
+#pragma unroll
+        for (int k = 1; k <= NO; ++k) {
+            float c = c_stag[nxo][k];
+            float pa = GXI(gxA, z, x + k - 1), pb = GXI(gxB, z, x + k - 1);
+            float ma, mb;
+            int Lm = x - k;
+            int nr = ordx(a, ix - k + 1, NO);
+            if (nr == ordx(a, ix - k, NO)) {
+                ma = GXI(gxA, z, Lm); mb = GXI(gxB, z, Lm);
+            } else {
+                float s1 = 0.f, s2 = 0.f;
+                for (int j = 1; j <= NO; ++j) {
+                    float cj = c_stag[nr][j];
+                    s1 = fmaf(cj, SU(sux, z, Lm + j) - SU(sux, z, Lm + 1 - j), s1);
+                    s2 = fmaf(cj, SU(suz, z, Lm + j) - SU(suz, z, Lm + 1 - j), s2);
+                }
+                ma = 2.0f / (SM(sRL2m, z, Lm) + SM(sRL2m, z, Lm + 1)) * s1;
+                mb = 2.0f / (SM(sRMu, z, Lm) + SM(sRMu, z, Lm + 1)) * s2;
+            }
+            x2a = fmaf(c, pa - ma, x2a);
+            x2b = fmaf(c, pb - mb, x2b);
+        }
+        const float Fx2_l2m_ux = x2a * dx2;
+        const float Fx2_mu_uz = x2b * dx2;
+
+        // z-direction second derivatives dzz(l2m uz), dzz(mu ux)
+        float z2a = 0.f, z2b = 0.f;
+#pragma unroll
+        for (int k = 1; k <= NO; ++k) {
+            float c = c_stag[nzo][k];
+            float pa = GZI(gzA, z + k - 1, x), pb = GZI(gzB, z + k - 1, x);
+            float ma, mb;
+            int Lm = z - k;
+            int nr = ordz(a, iz - k + 1, NO);
+            if (nr == ordz(a, iz - k, NO)) {
+                ma = GZI(gzA, Lm, x); mb = GZI(gzB, Lm, x);
+            } else {
+                float s1 = 0.f, s2 = 0.f;
+                for (int j = 1; j <= NO; ++j) {
+                    float cj = c_stag[nr][j];
+                    s1 = fmaf(cj, SU(suz, Lm + j, x) - SU(suz, Lm + 1 - j, x), s1);
+                    s2 = fmaf(cj, SU(sux, Lm + j, x) - SU(sux, Lm + 1 - j, x), s2);
+                }
+                ma = 2.0f / (SM(sRL2m, Lm, x) + SM(sRL2m, Lm + 1, x)) * s1;
+                mb = 2.0f / (SM(sRMu, Lm, x) + SM(sRMu, Lm + 1, x)) * s2;
+            }
+            z2a = fmaf(c, pa - ma, z2a);
+            z2b = fmaf(c, pb - mb, z2b);
+        }
+        const float Fz2_l2m_uz = z2a * a.dz2;
+        const float Fz2_mu_ux = z2b * a.dz2;
+
+        // mixed derivatives
+        float zxl = 0.f, zxm = 0.f, xzm = 0.f, xzl = 0.f;
+#pragma unroll
+        for (int k = 1; k <= NO; ++k) {
+            float cx = c_coll[nxo][k], cz = c_coll[nzo][k];
+            zxl = fmaf(cx, VXI(v1, z, x + k) - VXI(v1, z, x - k), zxl);
+            zxm = fmaf(cx, VXI(v4, z, x + k) - VXI(v4, z, x - k), zxm);
+            xzm = fmaf(cz, VZI(v2, z + k, x) - VZI(v2, z - k, x), xzm);
+            xzl = fmaf(cz, VZI(v3, z + k, x) - VZI(v3, z - k, x), xzl);
+        }
+        const float Fzx_lam_uz = zxl / dx, Fzx_mu_ux = zxm / dx;
+        const float Fxz_mu_uz = xzm / dz, Fxz_lam_ux = xzl / dz;
+
+        // free-surface terms on row 1 (stress image about row 1.5)
+        float fsA = 0.f, fsB = 0.f, fsx = 0.f, fsz = 0.f, dux1 = 0.f, duz1 = 0.f;
+        if (iz == 1) {
+            float dA = 0.f, dB = 0.f, dz1 = 0.f, dz2v = 0.f, dx1 = 0.f, dx2v = 0.f;
+#pragma unroll
+            for (int k = 1; k <= NO; ++k) {
+                float c = c_coll[nxo][k];
+                float Ap = SM(sLam, 0, x + k) * (SU(suz, 1, x + k) - SU(suz, 0, x + k)) / dz;
+                float Am = SM(sLam, 0, x - k) * (SU(suz, 1, x - k) - SU(suz, 0, x - k)) / dz;
+                float Bp = SM(sMu, 0, x + k) * (SU(sux, 1, x + k) - SU(sux, 0, x + k)) / dz;
+                float Bm = SM(sMu, 0, x - k) * (SU(sux, 1, x - k) - SU(sux, 0, x - k)) / dz;
+                dA = fmaf(c, Ap - Am, dA);
+                dB = fmaf(c, Bp - Bm, dB);
+                dz1 = fmaf(c, SU(suz, 0, x + k) - SU(suz, 0, x - k), dz1);
+                dz2v = fmaf(c, SU(suz, 1, x + k) - SU(suz, 1, x - k), dz2v);
+                dx1 = fmaf(c, SU(sux, 0, x + k) - SU(sux, 0, x - k), dx1);
+                dx2v = fmaf(c, SU(sux, 1, x + k) - SU(sux, 1, x - k), dx2v);
+            }
+            dA /= dx; dB /= dx; dz1 /= dx; dz2v /= dx; dx1 /= dx; dx2v /= dx;
+            const float mu1 = SM(sMu, 0, x), mu2 = SM(sMu, 1, x);
+            const float la1 = SM(sLam, 0, x), la2 = SM(sLam, 1, x);
+            const float hmu = 2.0f / (SM(sRMu, 0, x) + SM(sRMu, 1, x));
+            const float hl2m = 2.0f / (SM(sRL2m, 0, x) + SM(sRL2m, 1, x));
+            const float dux = SU(sux, 1, x) - SU(sux, 0, x);
+            const float duz = SU(suz, 1, x) - SU(suz, 0, x);
+            fsA = dA;                                   // Dx[lam(1) dz uz]
+            fsB = dB;                                   // Dx[mu(1)  dz ux]
+            fsx = hmu * dux / dz;                       // z part of sxz(1.5)
+            fsz = hl2m * duz / dz;                      // z part of szz(1.5)
+            // x parts of the half-row stresses
+            dux1 = 0.5f * (mu1 * dz1 + mu2 * dz2v);     // (mu1 Dx uz1 + mu2 Dx uz2)/2
+            duz1 = 0.5f * (la1 * dx1 + la2 * dx2v);     // (lam1 Dx ux1 + lam2 Dx ux2)/2
+        }
+
+        const float kd = __ldg(a.kdt2 + g);
+        float* uxn = a.ux[a.cur ^ 1];
+        float* uzn = a.uz[a.cur ^ 1];
+        const float ux0 = uxc[g], uz0 = uzc[g];
+
+        if (!pml) {
+            float Fx, Fz;
+            if (iz == 1) {
+                Fx = Fx2_l2m_ux + fsA + 2.0f * (fsx + dux1) / dz;
+                Fz = Fx2_mu_uz + fsB + 2.0f * (fsz + duz1) / dz;
+            } else {
+                Fx = Fx2_l2m_ux + Fzx_lam_uz + Fz2_mu_ux + Fxz_mu_uz;
+                Fz = Fz2_l2m_uz + Fxz_lam_ux + Fx2_mu_uz + Fzx_mu_ux;
+            }
+            uxn[g] = fmaf(kd, Fx, 2.0f * ux0 - uxn[g]);
+            uzn[g] = fmaf(kd, Fz, 2.0f * uz0 - uzn[g]);
+            continue;
+        }
+
+        // ---- PML cell: split-field update ----------------------------------
+        const int side = R.side;
+        const DampCol dxc = a.dampx[ix + npml - 1];
+        const DampCol dzc = side == 3 ? a.dampz[iz - 1] : DampCol{0.f, 0.f};
+        const float yx = dxc.y, yz = dzc.y;
+        size_t ap;
+        if (side == 1) ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - (1 - npml));
+        else if (side == 2) ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - nx - 1);
+        else ap = (size_t)(iz - nz - 1) + (size_t)npml * (size_t)(ix - (1 - npml));
+
+        // first derivatives for the memory variables (diff1 / diffx1 on the PML field)
+        float dxux = 0.f, dxuz = 0.f, dzux = 0.f, dzuz = 0.f;
+#pragma unroll
+        for (int k = 1; k <= NO; ++k) {
+            float cx = c_coll[nxo][k], cz = c_coll[nzo][k];
+            dxux = fmaf(cx, SU(sux, z, x + k) - SU(sux, z, x - k), dxux);
+            dxuz = fmaf(cx, SU(suz, z, x + k) - SU(suz, z, x - k), dxuz);
+            dzux = fmaf(cz, SU(sux, z + k, x) - SU(sux, z - k, x), dzux);
+            dzuz = fmaf(cz, SU(suz, z + k, x) - SU(suz, z - k, x), dzuz);
+        }
+        dxux /= dx; dxuz /= dx; dzux /= dz; dzuz /= dz;
+        const float lam0 = SM(sLam, z, x), mu0 = SM(sMu, z, x), l2m0 = SM(sL2m, z, x);
+
+        const int base = side == 1 ? 0 : side == 2 ? 6 : 12;
+        const int bpx0 = side == 1 ? 0 : side == 2 ? 2 : 8;
+        const int plane = a.cur, nplane = a.cur ^ 1;
+#pragma unroll
+        for (int comp = 0; comp < 2; ++comp) {
+            float F1, F2, F3, S1, S3 = 0.f;
+            if (iz == 1) {
+                if (comp == 0) {
+                    F1 = Fx2_l2m_ux;
+                    F2 = fsA + 2.0f * dux1 / dz;
+                    F3 = 2.0f * fsx / dz;
+                    S1 = l2m0 * dxux;
+                } else {
+                    F1 = Fx2_mu_uz;
+                    F2 = fsB + 2.0f * duz1 / dz;
+                    F3 = 2.0f * fsz / dz;
+                    S1 = mu0 * dxuz;
+                }
+            } else if (comp == 0) {
+                F1 = Fx2_l2m_ux;
+                F2 = Fzx_lam_uz + Fxz_mu_uz;
+                F3 = Fz2_mu_ux;
+                S1 = l2m0 * dxux;
+                S3 = mu0 * dzux;
+            } else {
+                F1 = Fx2_mu_uz;
+                F2 = Fxz_lam_ux + Fzx_mu_ux;
+                F3 = Fz2_l2m_uz;
+                S1 = mu0 * dxuz;
+                S3 = l2m0 * dzuz;
+            }
+            (void)lam0;
+            float* bpx = a.bp[side == 3 ? bpx0 + 2 * comp : bpx0 + comp];
+            const float Px = bpx[ap];
+            const float Pxn = ((1.0f - 0.5f * yx) * Px - dxc.dtdp * S1) / (1.0f + 0.5f * yx);
+            bpx[ap] = Pxn;
+            float* b1 = a.bu[base + 3 * comp + 0][plane];
+            float* b1n = a.bu[base + 3 * comp + 0][nplane];
+            float* b2 = a.bu[base + 3 * comp + 1][plane];
+            float* b2n = a.bu[base + 3 * comp + 1][nplane];
+            float* b3 = a.bu[base + 3 * comp + 2][plane];
+            float* b3n = a.bu[base + 3 * comp + 2][nplane];
+            const float u1 = b1[ap], u1m = b1n[ap];
+            const float f1 = kd * (F1 + 0.5f * (Pxn + Px));
+            float n1;
+            if (side == 2 && iz != 1)
+                n1 = ((2.0f - yx * yx) * u1 - (1.0f - yx) * u1m) / (1.0f + yx) + f1;
+            else
+                n1 = ((2.0f - yx * yx) * u1 - (1.0f - yx) * u1m + f1) / (1.0f + yx);
+            const float u2 = b2[ap], u2m = b2n[ap];
+            const float n2 = ((2.0f - yx * yz) * u2 - (1.0f - 0.5f * (yx + yz)) * u2m + kd * F2) / (1.0f + 0.5f * (yx + yz));
+            const float u3 = b3[ap], u3m = b3n[ap];
+            float n3;
+            if (side == 3) {
+                float* bpz = a.bp[9 + 2 * comp];
+                const float Pz = bpz[ap];
+                const float Pzn = ((1.0f - 0.5f * yz) * Pz - dzc.dtdp * S3) / (1.0f + 0.5f * yz);
+                bpz[ap] = Pzn;
+                n3 = ((2.0f - yz * yz) * u3 - (1.0f - yz) * u3m + kd * (F3 + 0.5f * (Pzn + Pz))) / (1.0f + yz);
+            } else {
+                n3 = fmaf(kd, F3, 2.0f * u3 - u3m);
+            }
+            b1n[ap] = n1;
+            b2n[ap] = n2;
+            b3n[ap] = n3;
+            if (comp == 0) uxn[g] = n1 + n2 + n3;
+            else uzn[g] = n1 + n2 + n3;
+        }
+    }
+#undef SU
+#undef SM
+#undef GXI
+#undef VXI
+#undef GZI
+#undef VZI
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launch helpers
+// ---------------------------------------------------------------------------
+template <int NO>
+static cudaError_t launch_no(const StepArgs& a, int n_sample_blocks, cudaStream_t s)
+{
+    size_t smem = sizeof(float) * (size_t)Tile<NO>::total;
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(fdfk_step_kernel<NO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    fdfk_step_kernel<NO><<<a.n_tiles + n_sample_blocks, kThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step(const StepArgs& a, cudaStream_t s)
+{
+    int nsb = a.nrcv > 0 ? (a.nrcv + kThreads - 1) / kThreads : 0;
+    switch (a.norder) {
+    case 1: return launch_no<1>(a, nsb, s);
+    case 2: return launch_no<2>(a, nsb, s);
+    case 3: return launch_no<3>(a, nsb, s);
+    case 4: return launch_no<4>(a, nsb, s);
+    case 5: return launch_no<5>(a, nsb, s);
+    case 6: return launch_no<6>(a, nsb, s);
+    case 7: return launch_no<7>(a, nsb, s);
+    case 8: return launch_no<8>(a, nsb, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+size_t step_smem_bytes(int norder)
+{
+    switch (norder) {
+    case 1: return sizeof(float) * Tile<1>::total;
+    case 2: return sizeof(float) * Tile<2>::total;
+    case 3: return sizeof(float) * Tile<3>::total;
+    case 4: return sizeof(float) * Tile<4>::total;
+    case 5: return sizeof(float) * Tile<5>::total;
+    case 6: return sizeof(float) * Tile<6>::total;
+    case 7: return sizeof(float) * Tile<7>::total;
+    case 8: return sizeof(float) * Tile<8>::total;
+    default: return 0;
+    }
+}
+
+cudaError_t set_coefficients(const float* stag, const float* coll)
+{
+    cudaError_t e = cudaMemcpyToSymbol(c_stag, stag, sizeof(float) * (kMaxOrder + 1) * (kMaxOrder + 1));
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyToSymbol(c_coll, coll, sizeof(float) * (kMaxOrder + 1) * (kMaxOrder + 1));
+}
+
+}  // namespace fdfk

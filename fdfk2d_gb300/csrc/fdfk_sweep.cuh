@@ -1,0 +1,69 @@
+// Device-side state and kernels of the hybrid FD-FK time step (sm_103a).
+//
+// One time step of FDFK2D's `updatedispl_` (call site src/FDFK2D.f90:516-522)
+// is one launch of fdfk_step_kernel<NO>.  The grid of CTAs is split into
+// interior tiles (rows 1..nz, columns 1..nx: leapfrog, Alterman-Karal
+// injection from the outer background strips, stress-image free surface) and
+// PML tiles (the absorbing frame: three-way split-field PML with memory
+// variables, injection by removing the inner background strips).  Receiver
+// sampling (loadseis, src/Submain.f90:33-116) runs in the same launch on
+// extra CTAs, reading the level that the step itself never writes.
+#pragma once
+#include <cstdint>
+
+namespace fdfk {
+
+constexpr int kMaxOrder = 8;   // FD order 16 (the reference caps norder at (npml+1)/2)
+constexpr int kTZ = 32;        // tile rows (z, the contiguous axis)
+constexpr int kTX = 32;        // tile columns (x)
+constexpr int kThreads = 256;  // 8 warps per CTA
+
+// Strip order = argument order of updatedispl_ (src/FDFK2D.f90:517-518).
+enum Strip { UXL_REG, UZL_REG, UXR_REG, UZR_REG, UXB_REG, UZB_REG,
+             UXL_PML, UZL_PML, UXR_PML, UZR_PML, UXB_PML, UZB_PML, NSTRIP };
+
+struct DampCol {   // per column (x) or row (z): d*dt and dt*d' for the PML
+    float y;       // d * dt
+    float dtdp;    // dt * dd/ds (signed along +x or +z)
+};
+
+struct StepArgs {
+    // geometry (izt = 1, free surface on top)
+    int nx, nz, npml, norder, nbd;
+    int NZ, NX, ldz;          // rows, columns, leading dimension (>= NZ, padded)
+    float dx, dz;
+    float dx2r, dx2p, dz2;    // 1/(dx*dx) as the regular (double-rounded) and PML (float) operators form it
+    float dt;
+    // material (column-major, ldz stride): k = dt^2/rho, lambda, mu
+    const float* __restrict__ kdt2;
+    const float* __restrict__ lam;
+    const float* __restrict__ mu;
+    // displacement planes [level parity]
+    float* ux[2];
+    float* uz[2];
+    // PML split fields bu[array][plane] (24 arrays in updatedispl_ order; top unused)
+    float* bu[24][2];
+    float* bp[12];
+    const DampCol* __restrict__ dampx;  // [NX]
+    const DampCol* __restrict__ dampz;  // [NZ]
+    // background strips (reference layout, time slowest), base of time 0
+    const float* __restrict__ strip[NSTRIP];
+    // tiles
+    int tiles_int_z, tiles_int_x;       // interior tiling
+    int tiles_l_z, tiles_l_x;           // left / right PML tiling (same shape)
+    int tiles_b_z, tiles_b_x;           // bottom PML tiling
+    int n_tiles;
+    // receivers sampled in the same launch (0 when this step takes no sample)
+    int nrcv;
+    int sample_index;          // istp
+    int nsamp;                 // nsis + 1 (leading dimension of seis)
+    float x0, z0;
+    const float* __restrict__ rx;
+    const float* __restrict__ rz;
+    float* seisx;
+    float* seisz;
+    int it;                    // time index of the background strips
+    int cur;                   // plane holding u^n (the other holds u^{n-1}, overwritten by u^{n+1})
+};
+
+}  // namespace fdfk

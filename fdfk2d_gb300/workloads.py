@@ -1,0 +1,178 @@
+"""Seeded synthetic workloads in the reference's input conventions (SI units).
+
+* :func:`config1` - 200 km x 100 km at 250 m (801 x 401), two layers
+  (crust 0-35 km Vp 6.3 / Vs 3.6 km/s over mantle Vp 8.1 / Vs 4.5 km/s),
+  20-cell PML, free surface, dt = 0.015 s, nt = 4000, 101 surface receivers
+  every 2 km, P incidence at 0.06 s/km, 1 Hz Ricker.
+* :func:`config2` - 400 km x 200 km at 100 m (4001 x 2001), 40-cell PML,
+  Moho dipping linearly 35 -> 55 km across the profile, a 60 km wide, 3 km
+  deep sediment basin (Vp 3.0 / Vs 1.5 km/s), a 3 % (std) Gaussian-smoothed
+  Vp/Vs perturbation with 5 km correlation length (seeded), dt = 0.006 s,
+  nt = 12000, 401 surface receivers, P incidence at 0.07 s/km.
+
+Density follows Gardner's rule rho = 1.74 Vp^0.25 g/cc with Vp in km/s
+(stored in kg/m^3).  FD order 6 (norder = 3) for both.
+
+:func:`plane_wave_background` fills the twelve background strips with an
+analytic P plane wave (Ricker wavelet) in the half-space below the model: a
+seeded stand-in for the FK background with the same shapes and value range,
+used where only the cost of the time loop matters.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .api import STRIPS, strip_shapes
+
+
+def gardner(vp):
+    return 1740.0 * (np.asarray(vp, np.float64) / 1000.0) ** 0.25
+
+
+def pack_c(vp, vs):
+    """c(1:3, NZ, NX) = rho, lambda, mu (src/Input.f90:364-378 with Gardner density)."""
+    rho = gardner(vp)
+    c = np.empty((3,) + vp.shape, np.float32, order="F")
+    c[0] = rho
+    c[1] = rho * (vp * vp - 2.0 * vs * vs)
+    c[2] = rho * vs * vs
+    return c
+
+
+def _smooth_noise(rng, NZ, NX, h, corr, std):
+    """Gaussian-smoothed white noise with correlation length `corr` (m), formed on a coarse grid."""
+    step = max(1, int(round(corr / h / 5)))
+    nzc, nxc = NZ // step + 3, NX // step + 3
+    w = rng.standard_normal((nzc, nxc))
+    sig = corr / (h * step)
+    r = int(math.ceil(3 * sig))
+    k = np.exp(-0.5 * (np.arange(-r, r + 1) / sig) ** 2)
+    k /= k.sum()
+    w = np.apply_along_axis(lambda v: np.convolve(v, k, mode="same"), 0, w)
+    w = np.apply_along_axis(lambda v: np.convolve(v, k, mode="same"), 1, w)
+    w = (w - w.mean()) / w.std() * std
+    zi = np.arange(NZ) / step
+    xi = np.arange(NX) / step
+    z0 = np.floor(zi).astype(int)
+    x0 = np.floor(xi).astype(int)
+    fz = (zi - z0)[:, None]
+    fx = (xi - x0)[None, :]
+    a = w[z0][:, x0]
+    b = w[z0 + 1][:, x0]
+    c = w[z0][:, x0 + 1]
+    d = w[z0 + 1][:, x0 + 1]
+    return (a * (1 - fz) * (1 - fx) + b * fz * (1 - fx) + c * (1 - fz) * fx + d * fz * fx)
+
+
+def _base(name, nx, nz, npml, h, dt, nt, nrcv, rayp_s_per_km, f0):
+    p = dict(norder=3, nx=nx, nz=nz, npml=npml, nt=nt, dx=h, dz=h, dt=dt, npower=2, R0=1e-3,
+             is_PML_top=False, nbd=5)
+    rx = np.linspace(0.0, (nx - 1) * h, nrcv).astype(np.float32)
+    rz = np.zeros(nrcv, np.float32)
+    return dict(name=name, p=p, rx=rx, rz=rz, x0=0.0, z0=0.0, nstp=1, nsis=nt,
+                rayp=rayp_s_per_km * 1e-3, f0=f0)
+
+
+def config1(nt=4000):
+    w = _base("config1: 200x100 km, 801x401 @ 250 m, 2 layers, P 0.06 s/km, nt=4000", 801, 401, 20, 250.0, 0.015,
+              nt, 101, 0.06, 1.0)
+    p = w["p"]
+    NZ, NX = p["nz"] + p["npml"], p["nx"] + 2 * p["npml"]
+    z = (np.arange(NZ) * p["dz"])[:, None] * np.ones((1, NX))
+    vp = np.where(z < 35e3, 6300.0, 8100.0)
+    vs = np.where(z < 35e3, 3600.0, 4500.0)
+    w["c"] = pack_c(vp, vs)
+    w["vp_half"] = 8100.0
+    p["vpml"] = float(vp.max())
+    return w
+
+
+def config2(nt=12000, seed=2024):
+    w = _base("config2: 400x200 km, 4001x2001 @ 100 m, dipping Moho + basin + 3% perturbation, P 0.07 s/km, "
+              "nt=12000", 4001, 2001, 40, 100.0, 0.006, nt, 401, 0.07, 1.0)
+    p = w["p"]
+    rng = np.random.default_rng(seed)
+    NZ, NX = p["nz"] + p["npml"], p["nx"] + 2 * p["npml"]
+    h = p["dx"]
+    x = ((np.arange(NX) - p["npml"]) * h)[None, :]
+    z = (np.arange(NZ) * h)[:, None]
+    L = (p["nx"] - 1) * h
+    moho = 35e3 + 20e3 * np.clip(x / L, 0.0, 1.0)
+    mantle = z >= moho
+    vp = np.where(mantle, 8100.0, 6300.0)
+    vs = np.where(mantle, 4500.0, 3600.0)
+    basin = (np.abs(x - 0.3 * L) <= 30e3) & (z < 3e3)
+    vp = np.where(basin, 3000.0, vp)
+    vs = np.where(basin, 1500.0, vs)
+    pert = _smooth_noise(rng, NZ, NX, h, 5e3, 0.03)
+    vp = vp * (1.0 + pert)
+    vs = vs * (1.0 + pert)
+    w["c"] = pack_c(vp, vs)
+    w["vp_half"] = 8100.0
+    p["vpml"] = float(vp.max())
+    return w
+
+
+def strip_coords(p, name):
+    """Fortran (iz, ix) of every element of a background strip (src/FDFK2D.f90:328-355)."""
+    nx, nz, nbd = p["nx"], p["nz"], p["nbd"]
+    side, kind = name[2], name[4:]
+    if kind == "reg":
+        if side == "l":
+            iz, ix = np.arange(1, nz - nbd + 1), np.arange(1, nbd + 1)
+        elif side == "r":
+            iz, ix = np.arange(1, nz - nbd + 1), np.arange(nx - nbd + 1, nx + 1)
+        else:
+            iz, ix = np.arange(nz - nbd + 1, nz + 1), np.arange(1, nx + 1)
+    else:
+        if side == "l":
+            iz, ix = np.arange(1, nz + 1), np.arange(1 - nbd, 1)
+        elif side == "r":
+            iz, ix = np.arange(1, nz + 1), np.arange(nx + 1, nx + nbd + 1)
+        else:
+            iz, ix = np.arange(nz + 1, nz + nbd + 1), np.arange(1 - nbd, nx + nbd + 1)
+    return iz, ix
+
+
+def plane_wave_background(w, t0_index=0, count=None, out=None, amp=1e-3):
+    """Analytic upgoing P plane wave on the strips for time indices [t0_index, t0_index + count).
+
+    Returns dict name -> float32 Fortran array (n1, n2, count) (or fills `out`, arrays of the same
+    shape, e.g. views of pinned buffers).  u = amp * ricker(t - tau) * (sin th, -cos th),
+    tau = t_s + p x - eta z, eta = sqrt(1/vp^2 - p^2).
+    """
+    p = w["p"]
+    if count is None:
+        count = p["nt"] + 1 - t0_index
+    vp = w["vp_half"]
+    ray = w["rayp"]
+    eta = math.sqrt(max(1.0 / vp ** 2 - ray ** 2, 0.0))
+    sin_t, cos_t = ray * vp, eta * vp
+    f0 = w["f0"]
+    zmax = (p["nz"] + p["npml"]) * p["dz"]
+    ts = 1.5 / f0 + eta * zmax
+    t = (np.arange(t0_index, t0_index + count) * p["dt"]).astype(np.float64)
+    res = {} if out is None else out
+    for name in STRIPS:
+        iz, ix = strip_coords(p, name)
+        x = w["x0"] + (ix - 1) * p["dx"]
+        z = w["z0"] + (iz - 1) * p["dz"]
+        tau = ts + ray * x[None, :] - eta * z[:, None]
+        arg = (np.pi * f0 * (t[None, None, :] - tau[:, :, None])) ** 2
+        val = amp * (1.0 - 2.0 * arg) * np.exp(-arg)
+        comp = sin_t if name[1] == "x" else -cos_t
+        v = (val * comp).astype(np.float32)
+        if out is None:
+            res[name] = np.asfortranarray(v)
+        else:
+            res[name][...] = v
+    return res
+
+
+def check_shapes(w, strips):
+    p = w["p"]
+    shp = strip_shapes(p["nx"], p["nz"], p["nbd"], p["nt"])
+    for k in STRIPS:
+        assert strips[k].shape[:2] == shp[k][:2], k

@@ -1,0 +1,155 @@
+/*
+ * fdfk_gb300: GB300 (sm_103a) replacement for the hot path of FDFK2D, the
+ * hybrid finite-difference / frequency-wavenumber teleseismic solver.
+ *
+ * The C ABI below is what the reference host (src/FDFK2D.f90) binds through
+ * iso_c_binding.  Plain pointers and sizes only; every array uses the
+ * reference's Fortran layout (column-major, the index ranges given per
+ * argument).  Every function returns FDFK_OK (0) or a negative status and
+ * never exits the process; fdfk_last_error() describes the last failure of
+ * the calling thread.
+ *
+ * Grid conventions (src/FDFK2D.f90:125, src/Input.f90:177-183):
+ *   NZ = nz + npml rows (iz = 1..nz+npml, free surface on top: izt = 1)
+ *   NX = nx + 2*npml columns (ix = 1-npml..nx+npml)
+ *   c(1:3, NZ, NX) = rho, lambda, mu
+ *   ux, uz (1:2, NZ, NX): level 1 = u^n, level 2 = u^{n-1}
+ *   background strips (12 arrays, time axis 0..nt last), shapes as allocated
+ *   in src/FDFK2D.f90:328-355, in the order of the updatedispl_ argument list:
+ *   uxl_reg uzl_reg uxr_reg uzr_reg uxb_reg uzb_reg uxl_pml uzl_pml uxr_pml
+ *   uzr_pml uxb_pml uzb_pml.
+ */
+#ifndef FDFK_GB300_H
+#define FDFK_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDFK_OK 0
+#define FDFK_EINVAL (-1)       /* bad argument or inconsistent sizes */
+#define FDFK_EUNSUPPORTED (-2) /* a mode this build does not implement */
+#define FDFK_ENOMEM (-3)       /* device or host allocation failed */
+#define FDFK_ECUDA (-4)        /* a CUDA call failed */
+#define FDFK_ESTATE (-5)       /* call out of order (e.g. no background yet) */
+
+/* Scalar arguments of updatedispl_ (src/FDFK2D.f90:516-519), same meaning. */
+typedef struct fdfk_params {
+    int norder;     /* half FD order, 1..8 */
+    int nx, nz;     /* interior grid */
+    int npml;       /* absorbing-layer width in cells (>= 2*norder-1) */
+    int is_PML_top; /* reference logical; only 0 (free surface) is implemented */
+    int npower;     /* damping profile exponent (reference: 2) */
+    int nbd;        /* background-strip width, 2*norder-1 */
+    int nt;         /* last time index; strips hold nt+1 samples */
+    float dx, dz;
+    double dt;
+    float vpml;     /* PML reference velocity (reference: max Vp) */
+    double R0;      /* target reflection coefficient (reference: 1e-3) */
+} fdfk_params;
+
+typedef struct fdfk_session fdfk_session;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int fdfk_version(void);
+
+/* Description of the last failure on this thread ("" if none). */
+const char* fdfk_last_error(void);
+
+/* Number of step-kernel launches issued by this process so far. */
+long long fdfk_kernel_launches(void);
+
+/*
+ * Create a solver session on the current CUDA device: allocates the resident
+ * wavefield, PML and material state in HBM and uploads c(1:3, NZ, NX).
+ * Replaces the allocations of simulate_wavefield (src/FDFK2D.f90:253-306)
+ * and the per-call copies of the material into the operators.
+ */
+int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out);
+
+/* Bind the session to a CUDA stream (cudaStream_t passed as void*; NULL = default). */
+int fdfk_session_set_stream(fdfk_session* s, void* stream);
+
+/*
+ * Upload background strips for time indices [t0, t0 + count) from the 12
+ * host arrays (full reference arrays covering 0..nt).  The strips are what
+ * comput_background_wavefield (src/FDFK2D.f90:432-434) produces.
+ */
+int fdfk_session_upload_background(fdfk_session* s, const float* const strips[12], int t0, int count);
+
+/*
+ * Receivers (src/Input.f90:227-249) and the sampling cadence of the time
+ * loop (src/FDFK2D.f90:311-315): a sample is taken before the step whenever
+ * it == istp*nstp, for istp = 0..nsis.
+ */
+int fdfk_session_set_receivers(fdfk_session* s, int nrcv, const float* rx, const float* rz, float x0, float z0,
+                               int nstp, int nsis);
+
+/*
+ * Advance `nsteps` time steps of the loop src/FDFK2D.f90:465-532
+ * (receiver sampling + updatedispl_), asynchronously on the session stream.
+ * The background for every step must have been uploaded.
+ */
+int fdfk_session_advance(fdfk_session* s, int nsteps);
+
+/* Time index of the next step (0 after create). */
+int fdfk_session_step_index(const fdfk_session* s);
+
+/* Wait for the session stream. */
+int fdfk_session_synchronize(fdfk_session* s);
+
+/* Copy the seismograms seisx/seisz(0:nsis, 1:nrcv) to host (radial component before
+ * the back-azimuth projection of src/FDFK2D.f90:537-542). */
+int fdfk_session_download_seismograms(fdfk_session* s, float* seisx, float* seisz);
+
+/* Copy samples [first, first + count) of every receiver into host arrays of
+ * shape (count, nrcv) (sample fastest). */
+int fdfk_session_download_seismogram_range(fdfk_session* s, int first, int count, float* seisx, float* seisz);
+
+/*
+ * Copy the full time-stepping state between host arrays in the reference
+ * layout and the device: ux, uz (1:2, NZ, NX); bp[12] and bu[24] in the
+ * updatedispl_ argument order (src/FDFK2D.f90:519-522; the four top-PML bp
+ * arrays and six top-PML bu arrays are unused with a free surface and may be
+ * NULL).  `it` sets the time index of the next step on upload.
+ */
+int fdfk_session_upload_state(fdfk_session* s, const float* ux, const float* uz, const float* const bp[12],
+                              const float* const bu[24], int it);
+int fdfk_session_download_state(fdfk_session* s, float* ux, float* uz, float* const bp[12], float* const bu[24]);
+
+void fdfk_session_destroy(fdfk_session* s);
+
+/*
+ * The whole time loop of simulate_wavefield (src/FDFK2D.f90:465-532) in one
+ * call: host material and background in, host seismograms out, state zeroed
+ * at the start as in src/FDFK2D.f90:280-300.  seisx/seisz are (nsis+1) x nrcv.
+ */
+int fdfk_simulate(const fdfk_params* p, const float* c, const float* const strips[12], int nrcv, const float* rx,
+                  const float* rz, float x0, float z0, int nstp, int nsis, float* seisx, float* seisz);
+
+/*
+ * Drop-in for the shipped libHybrid.so + libPML.so entry point
+ * `updatedispl_` (68 arguments, gfortran ABI, everything by reference),
+ * called from src/FDFK2D.f90:516-522.  Each call uploads the state, runs one
+ * fused step on the GPU and writes the state back into the caller's arrays.
+ * A mode this build does not implement prints a message and aborts, as the
+ * reference's `stop` would.
+ */
+void updatedispl_(const int* norder, const int* nx, const int* nz, const int* npml, const int* izt,
+                  const int* is_PML_top, const int* npower, const int* nbd, const int* it, const int* nt,
+                  const float* dx, const float* dz, const double* dt, const float* vpml, const double* R0,
+                  const float* uxl_reg, const float* uzl_reg, const float* uxr_reg, const float* uzr_reg,
+                  const float* uxb_reg, const float* uzb_reg, const float* uxl_pml, const float* uzl_pml,
+                  const float* uxr_pml, const float* uzr_pml, const float* uxb_pml, const float* uzb_pml,
+                  const float* c, const double* coef0, const double* coef1, float* ux, float* uz,
+                  float* bpxlx, float* bpzlx, float* bpxrx, float* bpzrx, float* bpxtx, float* bpxtz, float* bpztx,
+                  float* bpztz, float* bpxbx, float* bpxbz, float* bpzbx, float* bpzbz,
+                  float* bux1l, float* bux2l, float* bux3l, float* buz1l, float* buz2l, float* buz3l,
+                  float* bux1r, float* bux2r, float* bux3r, float* buz1r, float* buz2r, float* buz3r,
+                  float* bux1b, float* bux2b, float* bux3b, float* buz1b, float* buz2b, float* buz3b,
+                  float* bux1t, float* bux2t, float* bux3t, float* buz1t, float* buz2t, float* buz3t);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -156,6 +156,7 @@ void fdfk_op_diffzx_reg(int norder, int nx, int nz, int npml, int izt, float dx,
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
     size_t n = (size_t)g->ldz * g->ldx;
     float *v = (float *)calloc(n, sizeof(float));
+#pragma omp parallel for schedule(static)
     for (int iz = 2; iz <= nz; ++iz) {
         int no = IMIN(IMIN(iz - izt, nz + npml - iz), norder);
         for (int ix = 1 - norder; ix <= nx + norder; ++ix) {
@@ -165,6 +166,7 @@ void fdfk_op_diffzx_reg(int norder, int nx, int nz, int npml, int izt, float dx,
         }
     }
     memset(out, 0, n * sizeof(float));
+#pragma omp parallel for schedule(static)
     for (int ix = 1; ix <= nx; ++ix) {
         int no = IMIN(IMIN(ix + npml - 1, nx + npml - ix), norder);
         for (int iz = 2; iz <= nz; ++iz) {
@@ -192,6 +194,7 @@ void fdfk_op_diffzx_pml(int norder, int nx, int nz, int npml, int izt, float dx,
     size_t n = (size_t)g->ldz * g->ldx;
     float *v = (float *)calloc(n, sizeof(float));
     /* mask = 1; mask(1:nz, norder+1:nx-norder) = 0; mask(izt,:) = 0 */
+#pragma omp parallel for schedule(static)
     for (int iz = izt + 1; iz <= nz + npml - 1; ++iz) {
         int no = IMIN(IMIN(iz - izt, nz + npml - iz), norder);
         for (int ix = 2 - npml; ix <= nx + npml - 1; ++ix) {
@@ -203,6 +206,7 @@ void fdfk_op_diffzx_pml(int norder, int nx, int nz, int npml, int izt, float dx,
     }
     memset(out, 0, n * sizeof(float));
     /* mask = 1; mask(1:nz, 1:nx) = 0; mask(izt,:) = 0 */
+#pragma omp parallel for schedule(static)
     for (int ix = 2 - npml; ix <= nx + npml - 1; ++ix) {
         int no = IMIN(IMIN(ix + npml - 1, nx + npml - ix), norder);
         for (int iz = izt + 1; iz <= nz + npml - 1; ++iz) {
@@ -222,6 +226,7 @@ void fdfk_op_diffxz_reg(int norder, int nx, int nz, int npml, int izt, float dx,
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
     size_t n = (size_t)g->ldz * g->ldx;
     float *v = (float *)calloc(n, sizeof(float));
+#pragma omp parallel for schedule(static)
     for (int ix = 1; ix <= nx; ++ix) {
         int no = IMIN(IMIN(ix + npml - 1, nx + npml - ix), norder);
         for (int iz = 1; iz <= nz + norder; ++iz) {
@@ -231,6 +236,7 @@ void fdfk_op_diffxz_reg(int norder, int nx, int nz, int npml, int izt, float dx,
         }
     }
     memset(out, 0, n * sizeof(float));
+#pragma omp parallel for schedule(static)
     for (int iz = 2; iz <= nz; ++iz) {
         int no = IMIN(IMIN(iz - izt, nz + npml - iz), norder);
         for (int ix = 1; ix <= nx; ++ix) {
@@ -250,6 +256,7 @@ void fdfk_op_diffxz_pml(int norder, int nx, int nz, int npml, int izt, float dx,
     size_t n = (size_t)g->ldz * g->ldx;
     float *v = (float *)calloc(n, sizeof(float));
     /* mask = 1; mask(1:nz-norder, 1:nx) = 0 */
+#pragma omp parallel for schedule(static)
     for (int ix = 2 - npml; ix <= nx + npml - 1; ++ix) {
         int no = IMIN(IMIN(ix + npml - 1, nx + npml - ix), norder);
         for (int iz = izt; iz <= nz + npml - 1; ++iz) {
@@ -261,6 +268,7 @@ void fdfk_op_diffxz_pml(int norder, int nx, int nz, int npml, int izt, float dx,
     }
     memset(out, 0, n * sizeof(float));
     /* mask = 1; mask(1:nz, 1:nx) = 0; mask(izt,:) = 0 */
+#pragma omp parallel for schedule(static)
     for (int iz = izt + 1; iz <= nz + npml - 1; ++iz) {
         int no = IMIN(IMIN(iz - izt, nz + npml - iz), norder);
         for (int ix = 2 - npml; ix <= nx + npml - 1; ++ix) {
@@ -329,6 +337,7 @@ void fdfk_op_diffx2_reg(int norder, int nx, int nz, int npml, int izt, float dx,
     memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(float));
     float dx2 = (float)(1.0 / (double)(dx * dx));
     /* mask(1:nz, 1:nx) = 1, loop iz = izt..nz */
+#pragma omp parallel for schedule(static)
     for (int ix = 1; ix <= nx; ++ix)
         for (int iz = IMAX(izt, 1); iz <= nz; ++iz) G(out, iz, ix) = x2_point(g, norder, coef, mat, u, iz, ix) * dx2;
 }
@@ -340,6 +349,7 @@ void fdfk_op_diffx2_pml(int norder, int nx, int nz, int npml, int izt, float dx,
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
     memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(float));
     float dx2 = 1.0f / (dx * dx);
+#pragma omp parallel for schedule(static)
     for (int ix = 2 - npml; ix <= nx + npml - 1; ++ix)
         for (int iz = izt; iz <= nz + npml - 1; ++iz) {
             if (in_rect(iz, ix, 1, nz, 1, nx)) continue;
@@ -354,6 +364,7 @@ void fdfk_op_diffz2_reg(int norder, int nx, int nz, int npml, int izt, float dz,
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
     memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(float));
     float dz2 = 1.0f / (dz * dz);
+#pragma omp parallel for schedule(static)
     for (int iz = 2; iz <= nz; ++iz)
         for (int ix = 1; ix <= nx; ++ix) G(out, iz, ix) = z2_point(g, norder, coef, mat, u, iz, ix) * dz2;
 }
@@ -365,6 +376,7 @@ void fdfk_op_diffz2_pml(int norder, int nx, int nz, int npml, int izt, float dz,
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
     memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(float));
     float dz2 = 1.0f / (dz * dz);
+#pragma omp parallel for schedule(static)
     for (int iz = izt + 1; iz <= nz + npml - 1; ++iz)
         for (int ix = 1 - npml; ix <= nx + npml; ++ix) {
             if (in_rect(iz, ix, 1, nz, 1, nx)) continue;

@@ -1,0 +1,65 @@
+"""CPU tests of the C-ABI library: it builds for sm_103a, loads without a GPU, exports every
+symbol include/fdfk_gb300.h declares, and rejects bad arguments before touching the device."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "fdfk_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^[A-Za-z_][\w\s\*]*?\b(\w+)\s*\(", text, flags=re.M)) - {"defined"})
+
+
+@pytest.fixture(scope="module")
+def built():
+    from fdfk2d_gb300 import build
+    return build.build()
+
+
+def test_header_declares_the_entry_points():
+    names = declared_functions()
+    for must in ("fdfk_session_create", "fdfk_session_advance", "fdfk_simulate", "updatedispl_"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(built):
+    out = subprocess.run(["nm", "-D", "--defined-only", built], capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+
+
+def test_library_loads_and_validates_without_gpu(built):
+    import fdfk2d_gb300 as F
+    L = F.lib()
+    assert L.fdfk_version() >= 100
+    base = dict(norder=3, nx=40, nz=24, npml=8, nt=10, dx=250.0, dz=250.0, dt=0.015, vpml=8000.0)
+    c = np.ones((3, 32, 56), np.float32, order="F")
+    bad = [dict(norder=0), dict(norder=9), dict(npml=4), dict(nbd=4), dict(nz=5), dict(dx=0.0), dict(R0=2.0),
+           dict(nt=-1), dict(nx=6)]
+    for change in bad:
+        p = dict(base, **change)
+        with pytest.raises(F.FDFKError) as e:
+            F.Session(p, c)
+        assert e.value.code == -1, change
+    with pytest.raises(F.FDFKError) as e:
+        F.Session(dict(base, is_PML_top=True), c)
+    assert e.value.code == -2
+
+
+def test_shapes_match_reference_allocations():
+    import fdfk2d_gb300 as F
+    s = F.strip_shapes(40, 24, 5, 10)
+    assert s["uxl_reg"] == (19, 5, 11) and s["uxb_pml"] == (5, 50, 11)
+    ps = F.pml_shapes(40, 24, 8)
+    assert ps["bux1l"] == (2, 24, 8) and ps["bpxbx"] == (8, 56)
+    assert len(F.BU) == 24 and F.BU[0] == "bux1l" and F.BU[12] == "bux1b" and F.BU[18] == "bux1t"
