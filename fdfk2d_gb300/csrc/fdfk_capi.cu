@@ -15,6 +15,8 @@
 
 namespace fdfk {
 cudaError_t launch_step(const StepArgs& a, cudaStream_t s);
+cudaError_t launch_march(const StepArgs& a, const MarchArgs& m, cudaStream_t s);
+int march_warp_slots(int norder);
 cudaError_t set_coefficients(const float* stag, const float* coll);
 size_t step_smem_bytes(int norder);
 }  // namespace fdfk
@@ -101,6 +103,8 @@ struct fdfk_session {
     fdfk_params p{};
     int NZ = 0, NX = 0, ldz = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;     // second stream for the tiled kernel
+    cudaEvent_t fork = nullptr, join = nullptr;
     float* kdt2 = nullptr;
     float* lam = nullptr;
     float* mu = nullptr;
@@ -122,6 +126,7 @@ struct fdfk_session {
     float* seisx = nullptr;
     float* seisz = nullptr;
     StepArgs base{};
+    MarchArgs march{};
 };
 
 namespace {
@@ -145,6 +150,9 @@ int validate(const fdfk_params* p)
 void free_session(fdfk_session* s)
 {
     if (!s) return;
+    if (s->side) cudaStreamDestroy(s->side);
+    if (s->fork) cudaEventDestroy(s->fork);
+    if (s->join) cudaEventDestroy(s->join);
     cudaFree(s->kdt2); cudaFree(s->lam); cudaFree(s->mu);
     for (int l = 0; l < 2; ++l) { cudaFree(s->ux[l]); cudaFree(s->uz[l]); }
     for (int k = 0; k < 24; ++k) for (int l = 0; l < 2; ++l) cudaFree(s->bu[k][l]);
@@ -301,7 +309,39 @@ int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out
     a.kdt2 = s->kdt2; a.lam = s->lam; a.mu = s->mu;
     a.dampx = s->dampx; a.dampz = s->dampz;
     for (int k = 0; k < NSTRIP; ++k) a.strip[k] = s->strip[k];
-    a.tiles_int_z = (p->nz + kTZ - 1) / kTZ;
+    // Interior rows from 2*norder+1 down go to the marching fast path (orders <= kMarchMaxOrder): below
+    // them every stencil has its full order.
+    // FDFK_TILED_ONLY=1 keeps every cell on the tiled kernel (used to cross-check the two paths).
+    const char* tiled_only = std::getenv("FDFK_TILED_ONLY");
+    const bool march = p->norder <= kMarchMaxOrder && p->nz >= 2 * p->norder + 1 && !(tiled_only && tiled_only[0] == '1');
+    a.int_rows = march ? 2 * p->norder : p->nz;
+    s->march.z0 = 2 * p->norder + 1;
+    s->march.band_out = 64 - 4 * p->norder;
+    s->march.n_bands = march ? (p->nz - 2 * p->norder + s->march.band_out - 1) / s->march.band_out : 0;
+    // segments: one full wave of resident warps when the grid is large enough, else kMarchSeg columns
+    s->march.seg_len = kMarchSeg;
+    s->march.n_segs = march ? (p->nx + kMarchSeg - 1) / kMarchSeg : 0;
+    if (march) {
+        const int slots = march_warp_slots(p->norder);
+        if (slots > 0 && s->march.n_bands * s->march.n_segs > slots) {
+            const int segs = slots / s->march.n_bands;
+            if (segs >= 1 && (p->nx + segs - 1) / segs <= 4 * kMarchSeg) {
+                s->march.n_segs = segs;
+                s->march.seg_len = (p->nx + segs - 1) / segs;
+                s->march.n_segs = (p->nx + s->march.seg_len - 1) / s->march.seg_len;
+            }
+        }
+    }
+    if (march) {
+        cudaError_t e1 = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+        cudaError_t e2 = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
+        cudaError_t e3 = cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+            free_session(s);
+            return fail(FDFK_ECUDA, "stream/event creation failed");
+        }
+    }
+    a.tiles_int_z = (a.int_rows + kTZ - 1) / kTZ;
     a.tiles_int_x = (p->nx + kTX - 1) / kTX;
     a.tiles_l_z = (p->nz + kTZ - 1) / kTZ;
     a.tiles_l_x = (p->npml + kTX - 1) / kTX;
@@ -387,9 +427,23 @@ int fdfk_session_advance(fdfk_session* s, int nsteps)
             s->istp += 1;
             s->isis += s->nstp;
         }
-        cudaError_t e = launch_step(a, s->stream);
-        if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("step launch: ") + cudaGetErrorString(e));
-        g_launches.fetch_add(1);
+        if (s->march.n_bands > 0) {
+            // The two kernels write disjoint cells and read only u^n: run the tiled one (top band,
+            // PML, receivers) on a side stream next to the interior fast path.
+            CK(cudaEventRecord(s->fork, s->stream));
+            CK(cudaStreamWaitEvent(s->side, s->fork, 0));
+            cudaError_t e = launch_step(a, s->side);
+            if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("step launch: ") + cudaGetErrorString(e));
+            e = launch_march(a, s->march, s->stream);
+            if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("march launch: ") + cudaGetErrorString(e));
+            CK(cudaEventRecord(s->join, s->side));
+            CK(cudaStreamWaitEvent(s->stream, s->join, 0));
+            g_launches.fetch_add(2);
+        } else {
+            cudaError_t e = launch_step(a, s->stream);
+            if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("step launch: ") + cudaGetErrorString(e));
+            g_launches.fetch_add(1);
+        }
         s->cur ^= 1;
         s->it += 1;
     }

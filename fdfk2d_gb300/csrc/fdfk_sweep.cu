@@ -46,6 +46,14 @@ struct Rect {
     int zlo, zhi, xlo, xhi;  // output rectangle (inclusive)
 };
 
+// Reciprocal to within 1 ulp (MUFU); the reference's IEEE divisions agree to rounding.
+__device__ __forceinline__ float fast_rcp(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 __device__ __forceinline__ int ordx(const StepArgs& a, int ix, int NO)
 {
     int n = min(min(ix + a.npml - 1, a.nx + a.npml - ix), NO);
@@ -108,7 +116,7 @@ __device__ __forceinline__ Rect decode_tile(const StepArgs& a, int b)
     if (b < ni) {
         r.side = 0;
         r.z0 = 1 + (b % a.tiles_int_z) * kTZ; r.x0 = 1 + (b / a.tiles_int_z) * kTX;
-        r.zlo = 1; r.zhi = a.nz; r.xlo = 1; r.xhi = a.nx;
+        r.zlo = 1; r.zhi = a.int_rows; r.xlo = 1; r.xhi = a.nx;
         return r;
     }
     b -= ni;
@@ -204,6 +212,7 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
     float* v2 = gzB + T::AZ;    // mu  * Dx(uz)/dx        [x][z]  (dxz(mu uz))
     float* v3 = v2 + T::AZ;     // lam * Dx(ux)/dx                 (dxz(lam ux))
 
+    const float rdx = 1.0f / a.dx, rdz = 1.0f / a.dz;
     const float* uxc = a.ux[a.cur];
     const float* uzc = a.uz[a.cur];
 
@@ -241,8 +250,8 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
         sLam[i] = l;
         sMu[i] = m;
         sL2m[i] = l2;
-        sRL2m[i] = 1.0f / l2;
-        sRMu[i] = 1.0f / m;
+        sRL2m[i] = fast_rcp(l2);
+        sRMu[i] = fast_rcp(m);
     }
     __syncthreads();
 
@@ -264,8 +273,8 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
                 sx = fmaf(c, SU(sux, z, L + j) - SU(sux, z, L + 1 - j), sx);
                 szv = fmaf(c, SU(suz, z, L + j) - SU(suz, z, L + 1 - j), szv);
             }
-            float hl = 2.0f / (SM(sRL2m, z, L) + SM(sRL2m, z, L + 1));
-            float hm = 2.0f / (SM(sRMu, z, L) + SM(sRMu, z, L + 1));
+            float hl = 2.0f * fast_rcp(SM(sRL2m, z, L) + SM(sRL2m, z, L + 1));
+            float hm = 2.0f * fast_rcp(SM(sRMu, z, L) + SM(sRMu, z, L + 1));
             gxA[i] = hl * sx;
             gxB[i] = hm * szv;
         }
@@ -284,8 +293,8 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
             // diffzx_reg forms v on rows 2..nz; diffzx_pml on rows 2..NZ-1, columns 2-npml..nx+npml-1
             bool valid = pml ? (iz >= 2 && iz <= NZ - 1 && ix >= 2 - npml && ix <= nx + npml - 1)
                              : (iz >= 2 && iz <= nz && ix >= 1 - NO && ix <= nx + NO);
-            v1[i] = valid ? SM(sLam, z, x) * dzz / a.dz : 0.f;
-            v4[i] = valid ? SM(sMu, z, x) * dzx / a.dz : 0.f;
+            v1[i] = valid ? SM(sLam, z, x) * dzz * rdz : 0.f;
+            v4[i] = valid ? SM(sMu, z, x) * dzx * rdz : 0.f;
         }
     }
     // ---- phase 1b: z-direction staggered products and dxz operands -----------
@@ -302,8 +311,8 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
                 sz_ = fmaf(c, SU(suz, L + j, x) - SU(suz, L + 1 - j, x), sz_);
                 sx = fmaf(c, SU(sux, L + j, x) - SU(sux, L + 1 - j, x), sx);
             }
-            float hl = 2.0f / (SM(sRL2m, L, x) + SM(sRL2m, L + 1, x));
-            float hm = 2.0f / (SM(sRMu, L, x) + SM(sRMu, L + 1, x));
+            float hl = 2.0f * fast_rcp(SM(sRL2m, L, x) + SM(sRL2m, L + 1, x));
+            float hm = 2.0f * fast_rcp(SM(sRMu, L, x) + SM(sRMu, L + 1, x));
             gzA[i] = hl * sz_;
             gzB[i] = hm * sx;
         }
@@ -321,8 +330,8 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
             // diffxz_reg forms v on rows 1..nz+norder, columns 1..nx; diffxz_pml on rows 1..NZ-1
             bool valid = pml ? (iz >= 1 && iz <= NZ - 1 && ix >= 2 - npml && ix <= nx + npml - 1)
                              : (iz >= 1 && iz <= nz + NO && ix >= 1 && ix <= nx);
-            v2[i] = valid ? SM(sMu, z, x) * dxz / a.dx : 0.f;
-            v3[i] = valid ? SM(sLam, z, x) * dxx / a.dx : 0.f;
+            v2[i] = valid ? SM(sMu, z, x) * dxz * rdx : 0.f;
+            v3[i] = valid ? SM(sLam, z, x) * dxx * rdx : 0.f;
         }
     }
     __syncthreads();
@@ -416,8 +425,8 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
             xzm = fmaf(cz, VZI(v2, z + k, x) - VZI(v2, z - k, x), xzm);
             xzl = fmaf(cz, VZI(v3, z + k, x) - VZI(v3, z - k, x), xzl);
         }
-        const float Fzx_lam_uz = zxl / dx, Fzx_mu_ux = zxm / dx;
-        const float Fxz_mu_uz = xzm / dz, Fxz_lam_ux = xzl / dz;
+        const float Fzx_lam_uz = zxl * rdx, Fzx_mu_ux = zxm * rdx;
+        const float Fxz_mu_uz = xzm * rdz, Fxz_lam_ux = xzl * rdz;
 
         // free-surface terms on row 1 (stress image about row 1.5)
         float fsA = 0.f, fsB = 0.f, fsx = 0.f, fsz = 0.f, dux1 = 0.f, duz1 = 0.f;
@@ -628,3 +637,6 @@ cudaError_t set_coefficients(const float* stag, const float* coll)
 }
 
 }  // namespace fdfk
+
+// The interior fast path shares the coefficient tables above.
+#include "fdfk_march.cuh"

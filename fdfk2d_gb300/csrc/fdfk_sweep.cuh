@@ -49,6 +49,7 @@ struct StepArgs {
     // background strips (reference layout, time slowest), base of time 0
     const float* __restrict__ strip[NSTRIP];
     // tiles
+    int int_rows;                       // interior rows [1, int_rows] handled by the tiled kernel
     int tiles_int_z, tiles_int_x;       // interior tiling
     int tiles_l_z, tiles_l_x;           // left / right PML tiling (same shape)
     int tiles_b_z, tiles_b_x;           // bottom PML tiling
@@ -65,5 +66,17 @@ struct StepArgs {
     int it;                    // time index of the background strips
     int cur;                   // plane holding u^n (the other holds u^{n-1}, overwritten by u^{n+1})
 };
+
+// Interior fast path (fdfk_march_kernel): rows [z0, nz], columns [1, nx].
+struct MarchArgs {
+    int z0;          // first output row (odd, >= 2*norder + 1)
+    int band_out;    // output rows per warp band (64 - 4*norder)
+    int n_bands;
+    int seg_len;     // columns per warp segment
+    int n_segs;
+};
+
+constexpr int kMarchSeg = 64;
+constexpr int kMarchMaxOrder = 4;
 
 }  // namespace fdfk
