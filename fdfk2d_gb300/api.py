@@ -69,7 +69,8 @@ def lib():
                      "fdfk_session_step_index", "fdfk_session_destroy", "fdfk_session_upload_background",
                      "fdfk_session_set_receivers", "fdfk_session_download_seismograms",
                      "fdfk_session_upload_state", "fdfk_session_download_state",
-                     "fdfk_session_download_seismogram_range"):
+                     "fdfk_session_download_seismogram_range", "fdfk_session_advance_timed",
+                     "fdfk_session_interior_cells"):
             getattr(L, name).restype = C.c_int if name != "fdfk_session_destroy" else None
         _lib = L
     return _lib
@@ -160,6 +161,18 @@ class Session:
 
     def advance(self, nsteps: int):
         _check(lib().fdfk_session_advance(self._h, C.c_int(nsteps)))
+
+    def advance_timed(self, nsteps: int):
+        """Advance with CUDA events around each kernel; returns (ms_interior, ms_edge) summed."""
+        ti, te = C.c_float(), C.c_float()
+        _check(lib().fdfk_session_advance_timed(self._h, C.c_int(nsteps), C.byref(ti), C.byref(te)))
+        return float(ti.value), float(te.value)
+
+    def cell_split(self):
+        """(cells on the interior fast path, cells on the tiled kernel) per step."""
+        i, e = C.c_longlong(), C.c_longlong()
+        _check(lib().fdfk_session_interior_cells(self._h, C.byref(i), C.byref(e)))
+        return int(i.value), int(e.value)
 
     @property
     def step_index(self) -> int:

@@ -450,6 +450,77 @@ int fdfk_session_advance(fdfk_session* s, int nsteps)
     return FDFK_OK;
 }
 
+int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, float* ms_edge)
+{
+    if (!s || !ms_interior || !ms_edge) return fail(FDFK_EINVAL, "NULL argument");
+    *ms_interior = 0.f;
+    *ms_edge = 0.f;
+    if (nsteps <= 0) return fdfk_session_advance(s, nsteps);
+    const bool two = s->march.n_bands > 0;
+    std::vector<cudaEvent_t> ev((size_t)nsteps * 4, nullptr);
+    auto cleanup = [&]() { for (auto e : ev) if (e) cudaEventDestroy(e); };
+    for (auto& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) { cleanup(); return fail(FDFK_ECUDA, "event creation failed"); }
+    for (int k = 0; k < nsteps; ++k) {
+        const int it = s->it;
+        if (it > s->p.nt) { cleanup(); return fail(FDFK_EINVAL, "advance past the last time index nt"); }
+        if (!s->have_bg[it]) { cleanup(); return fail(FDFK_ESTATE, "no background uploaded for time index " + std::to_string(it)); }
+        StepArgs a = s->base;
+        for (int l = 0; l < 2; ++l) { a.ux[l] = s->ux[l]; a.uz[l] = s->uz[l]; }
+        for (int q = 0; q < 24; ++q) for (int l = 0; l < 2; ++l) a.bu[q][l] = s->bu[q][l];
+        for (int q = 0; q < 12; ++q) a.bp[q] = s->bp[q];
+        a.it = it;
+        a.cur = s->cur;
+        a.nrcv = 0;
+        if (s->nrcv > 0 && s->isis == it && s->istp <= s->nsis) {
+            a.nrcv = s->nrcv; a.sample_index = s->istp; a.nsamp = s->nsis + 1;
+            a.x0 = s->x0; a.z0 = s->z0; a.rx = s->rx; a.rz = s->rz; a.seisx = s->seisx; a.seisz = s->seisz;
+            s->istp += 1;
+            s->isis += s->nstp;
+        }
+        cudaEvent_t* e = &ev[(size_t)k * 4];
+        cudaStream_t edge = two ? s->side : s->stream;
+        if (two) {
+            cudaEventRecord(s->fork, s->stream);
+            cudaStreamWaitEvent(s->side, s->fork, 0);
+        }
+        cudaEventRecord(e[2], edge);
+        cudaError_t r = launch_step(a, edge);
+        cudaEventRecord(e[3], edge);
+        if (r == cudaSuccess && two) {
+            cudaEventRecord(e[0], s->stream);
+            r = launch_march(a, s->march, s->stream);
+            cudaEventRecord(e[1], s->stream);
+            cudaEventRecord(s->join, s->side);
+            cudaStreamWaitEvent(s->stream, s->join, 0);
+        }
+        if (r != cudaSuccess) { cleanup(); return fail(FDFK_ECUDA, std::string("launch: ") + cudaGetErrorString(r)); }
+        g_launches.fetch_add(two ? 2 : 1);
+        s->cur ^= 1;
+        s->it += 1;
+    }
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) { cleanup(); return fail(FDFK_ECUDA, "synchronize failed"); }
+    double ti = 0.0, te = 0.0;
+    for (int k = 0; k < nsteps; ++k) {
+        float t = 0.f;
+        if (two && cudaEventElapsedTime(&t, ev[(size_t)k * 4], ev[(size_t)k * 4 + 1]) == cudaSuccess) ti += t;
+        if (cudaEventElapsedTime(&t, ev[(size_t)k * 4 + 2], ev[(size_t)k * 4 + 3]) == cudaSuccess) te += t;
+    }
+    cleanup();
+    *ms_interior = (float)ti;
+    *ms_edge = (float)te;
+    return FDFK_OK;
+}
+
+int fdfk_session_interior_cells(const fdfk_session* s, long long* interior, long long* edge)
+{
+    if (!s || !interior || !edge) return fail(FDFK_EINVAL, "NULL argument");
+    const long long total = (long long)s->NZ * s->NX;
+    *interior = s->march.n_bands > 0 ? (long long)(s->p.nz - 2 * s->p.norder) * s->p.nx : 0;
+    *edge = total - *interior;
+    return FDFK_OK;
+}
+
 int fdfk_session_step_index(const fdfk_session* s) { return s ? s->it : FDFK_EINVAL; }
 
 int fdfk_session_synchronize(fdfk_session* s)

@@ -3,18 +3,27 @@
 //
 // Each warp owns a band of 64 rows (2 per lane; z is the contiguous axis, so
 // every global access of a warp is one contiguous 256-byte run) and marches
-// along x over a segment of columns.  x-direction stencils live in register
-// windows that slide with the march; z-direction stencils read neighbouring
-// rows with warp shuffles.  Nothing goes through shared memory and there is
-// no block-level synchronisation.  The 2*norder halo rows on each side of a
-// band are computed but not stored; bands overlap accordingly.  The first
-// 2*norder march steps of a segment only fill the windows.
+// along x over a segment of columns, reading each field column once.  The
+// x-direction stencils are evaluated in transposed (accumulator) form: every
+// incoming column is folded with one FMA per stencil tap into a short chain of
+// partial sums that advances with the march, so no operand windows are kept
+// or shifted.  z-direction stencils read neighbouring rows with warp shuffles,
+// one shuffle per distinct neighbour row.  Nothing goes through shared memory
+// and there is no block-level synchronisation.  The 2*norder halo rows on
+// each side of a band are computed but not stored; bands overlap accordingly.
+//
+// With newest column m, the pipeline delivers
+//   S(h) = staggered x-derivative at half point h = m - NO + 1/2   (lag NO - 1/2)
+//   Dx u  collocated x-derivative at column m - NO                  (lag NO)
+//   V     = M Dz u / dz at column m                                  (lag 0)
+// and accumulates the force of cells m - 2NO + 1 .. m + NO; cell
+// m - 2NO + 1 is complete and is advanced in time.
 //
 // Semantics are those of fdfk_step_kernel's interior tiles with full stencil
 // orders (src/Submain.f90 diffx2/diffz2/diffxz/diffzx *_reg): the fast path
 // starts below the rows where the top boundary reduces the order, and the
-// outer background strips (Omega_II) are added to every loaded value that lies
-// on them (Alterman-Karal injection).
+// outer background strips (Omega_II) are added to every loaded value that
+// lies on them (Alterman-Karal injection).
 //
 // Included by fdfk_sweep.cu after the coefficient tables c_stag / c_coll are
 // defined: constant memory is per translation unit without relocatable
@@ -49,52 +58,63 @@ __device__ __forceinline__ float zrow(float a0, float a1)
     else return __shfl_up_sync(kFull, v, -q);
 }
 
-// Collocated z-derivative sums (no 1/dz) of a column at this lane's two rows.
-template <int NO>
-__device__ __forceinline__ void dz_coll(float v0, float v1, float& d0, float& d1)
-{
-    float s0 = 0.f, s1 = 0.f;
-#define FDFK_DZ(k)                                                                          \
-    if constexpr (NO >= k) {                                                                \
-        s0 = fmaf(c_coll[NO][k], zrow<k>(v0, v1) - zrow<-(k)>(v0, v1), s0);               \
-        s1 = fmaf(c_coll[NO][k], zrow<(k) + 1>(v0, v1) - zrow<1 - (k)>(v0, v1), s1);      \
+// Rows r0+LO .. r0+HI of a two-rows-per-lane quantity (one shuffle per row not held by this lane).
+template <int LO, int HI>
+struct ZCol {
+    float v[HI - LO + 1];
+    __device__ __forceinline__ ZCol(float a0, float a1) { fill<LO>(a0, a1); }
+    template <int D>
+    __device__ __forceinline__ void fill(float a0, float a1)
+    {
+        if constexpr (D <= HI) {
+            v[D - LO] = zrow<D>(a0, a1);
+            fill<D + 1>(a0, a1);
+        }
     }
-    FDFK_DZ(1) FDFK_DZ(2) FDFK_DZ(3) FDFK_DZ(4)
-#undef FDFK_DZ
+    __device__ __forceinline__ float operator()(int d) const { return v[d - LO]; }
+};
+
+// sum_k c1_k (q(r+k) - q(r-k)) at this lane's two rows
+template <int NO>
+__device__ __forceinline__ void dz_coll(float a0, float a1, float& d0, float& d1)
+{
+    const ZCol<-NO, NO + 1> z(a0, a1);
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+    for (int k = 1; k <= NO; ++k) {
+        s0 = fmaf(c_coll[NO][k], z(k) - z(-k), s0);
+        s1 = fmaf(c_coll[NO][k], z(k + 1) - z(1 - k), s1);
+    }
     d0 = s0;
     d1 = s1;
 }
 
-// Staggered z-derivative sums at the half rows below this lane's rows
-// (label L between rows L and L+1, for L = r0 and r0+1).
+// sum_j c0_j (q(L+j) - q(L+1-j)) at the half rows L = r0, r0+1 (label = upper row)
 template <int NO>
-__device__ __forceinline__ void dz_stag(float v0, float v1, float& d0, float& d1)
+__device__ __forceinline__ void dz_stag(float a0, float a1, float& d0, float& d1)
 {
+    const ZCol<1 - NO, NO + 1> z(a0, a1);
     float s0 = 0.f, s1 = 0.f;
-#define FDFK_DS(j)                                                                          \
-    if constexpr (NO >= j) {                                                                \
-        s0 = fmaf(c_stag[NO][j], zrow<j>(v0, v1) - zrow<1 - (j)>(v0, v1), s0);            \
-        s1 = fmaf(c_stag[NO][j], zrow<(j) + 1>(v0, v1) - zrow<2 - (j)>(v0, v1), s1);      \
+#pragma unroll
+    for (int j = 1; j <= NO; ++j) {
+        s0 = fmaf(c_stag[NO][j], z(j) - z(1 - j), s0);
+        s1 = fmaf(c_stag[NO][j], z(j + 1) - z(2 - j), s1);
     }
-    FDFK_DS(1) FDFK_DS(2) FDFK_DS(3) FDFK_DS(4)
-#undef FDFK_DS
     d0 = s0;
     d1 = s1;
 }
 
-// Staggered z-derivative of half-row quantities G (label = upper row) at this lane's rows:
-// sum_k c_k (G(r+k-1) - G(r-k)).
+// sum_k c0_k (G(r+k-1) - G(r-k)) of half-row quantities G at this lane's rows
 template <int NO>
-__device__ __forceinline__ void dz_of_half(float g0, float g1, float& d0, float& d1)
+__device__ __forceinline__ void dz_half(float g0, float g1, float& d0, float& d1)
 {
+    const ZCol<-NO, NO> z(g0, g1);
     float s0 = 0.f, s1 = 0.f;
-#define FDFK_DH(k)                                                                          \
-    if constexpr (NO >= k) {                                                                \
-        s0 = fmaf(c_stag[NO][k], zrow<(k) - 1>(g0, g1) - zrow<-(k)>(g0, g1), s0);         \
-        s1 = fmaf(c_stag[NO][k], zrow<(k)>(g0, g1) - zrow<1 - (k)>(g0, g1), s1);          \
+#pragma unroll
+    for (int k = 1; k <= NO; ++k) {
+        s0 = fmaf(c_stag[NO][k], z(k - 1) - z(-k), s0);
+        s1 = fmaf(c_stag[NO][k], z(k) - z(1 - k), s1);
     }
-    FDFK_DH(1) FDFK_DH(2) FDFK_DH(3) FDFK_DH(4)
-#undef FDFK_DH
     d0 = s0;
     d1 = s1;
 }
@@ -105,9 +125,10 @@ template <int NO>
 __global__ void __launch_bounds__(128) fdfk_march_kernel(StepArgs a, MarchArgs m)
 {
     using namespace march;
-    constexpr int W = 3 * NO;        // field window: columns x-NO .. x+2NO-1
-    constexpr int WG = 2 * NO;       // staggered products: half points x-NO+1/2 .. x+NO-1/2
-    constexpr int WV = 2 * NO + 1;   // dzx operands: columns x-NO .. x+NO
+    constexpr int NS = 2 * NO;       // staggered partial sums: half points m-NO+1/2 .. m+NO-1/2
+    constexpr int ND = 2 * NO + 1;   // collocated partial sums: columns m-NO .. m+NO
+    constexpr int NF = 3 * NO;       // force accumulators: cells m-2NO+1 .. m+NO
+    constexpr int LAG = 2 * NO - 1;  // newest column minus completed cell
 
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * (blockDim.x >> 5)) + (threadIdx.x >> 5);
@@ -133,8 +154,10 @@ __global__ void __launch_bounds__(128) fdfk_march_kernel(StepArgs a, MarchArgs m
     const float rdx = 1.0f / a.dx, rdz = 1.0f / a.dz;
     const float dx2 = a.dx2r, dz2 = a.dz2;
 
-    auto colbase = [&](int ix) -> size_t { return (size_t)(ix + npml - 1) * (size_t)ldz + (size_t)(r0 - 1); };
-    auto load_pair = [&](const float* __restrict__ p, size_t o, float& v0, float& v1) {
+    // element offset of (r0, column ix); 32-bit: grids are below 2^31 cells
+    const int rowoff = r0 - 1;
+    auto colbase = [&](int ix) -> int { return (ix + npml - 1) * ldz + rowoff; };
+    auto load_pair = [&](const float* __restrict__ p, int o, float& v0, float& v1) {
         if (rows_in) {
             const float2 v = __ldg(reinterpret_cast<const float2*>(p + o));
             v0 = v.x; v1 = v.y;
@@ -146,7 +169,7 @@ __global__ void __launch_bounds__(128) fdfk_march_kernel(StepArgs a, MarchArgs m
     // field column with the Omega_II background added; zero outside the grid
     auto load_u = [&](int ix, float& x0, float& x1, float& z0, float& z1) {
         if (ix < 1 - npml || ix > nx + npml) { x0 = x1 = z0 = z1 = 0.f; return; }
-        const size_t o = colbase(ix);
+        const int o = colbase(ix);
         load_pair(uxc, o, x0, x1);
         load_pair(uzc, o, z0, z1);
         if ((ix <= 0 && ix >= 1 - nbd) || (ix > nx && ix <= nx + nbd)) {
@@ -173,7 +196,7 @@ __global__ void __launch_bounds__(128) fdfk_march_kernel(StepArgs a, MarchArgs m
     };
     auto load_mat = [&](int ix, float& l0, float& l1, float& m0, float& m1) {
         if (ix < 1 - npml || ix > nx + npml) { l0 = l1 = 0.f; m0 = m1 = 1.f; return; }
-        const size_t o = colbase(ix);
+        const int o = colbase(ix);
         if (rows_in) {
             const float2 l = __ldg(reinterpret_cast<const float2*>(a.lam + o));
             const float2 mm = __ldg(reinterpret_cast<const float2*>(a.mu + o));
@@ -186,159 +209,193 @@ __global__ void __launch_bounds__(128) fdfk_march_kernel(StepArgs a, MarchArgs m
         }
     };
 
-    float Ux[W][2], Uz[W][2];        // column x - NO + c
-    float Ga[WG][2], Gb[WG][2];      // H(l2m) Dstag_x ux, H(mu) Dstag_x uz at half point x - NO + 1/2 + c
-    float V1[WV][2], V4[WV][2];      // lam Dz uz / dz, mu Dz ux / dz at column x - NO + c
-    float RL0[2], RL1[2], RM0[2], RM1[2];   // 1/l2m, 1/mu at columns x+NO-1 (0) and x+NO (1)
-
-    // prologue: field columns x0-NO .. x0+2NO-2 and the reciprocals of column x0+NO-1
-    const int x0 = xs - 2 * NO;
+    // accumulator chains (index 0 = oldest), [row]
+    float SA[NS][2], SB[NS][2];      // staggered d/dx of ux, uz
+    float D2[ND][2], D3[ND][2];      // collocated d/dx of uz, ux
+    float FX[NF][2], FZ[NF][2];      // forces
 #pragma unroll
-    for (int c = 0; c < W - 1; ++c) load_u(x0 - NO + c, Ux[c][0], Ux[c][1], Uz[c][0], Uz[c][1]);
+    for (int i = 0; i < NS; ++i) SA[i][0] = SA[i][1] = SB[i][0] = SB[i][1] = 0.f;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) D2[i][0] = D2[i][1] = D3[i][0] = D3[i][1] = 0.f;
+#pragma unroll
+    for (int i = 0; i < NF; ++i) FX[i][0] = FX[i][1] = FZ[i][0] = FZ[i][1] = 0.f;
+
+    // reciprocals of l2m and mu at the lagged column m-NO (left of the emitted half point)
+    float rlp0 = 1.f, rlp1 = 1.f, rmp0 = 1.f, rmp1 = 1.f;
+    // lam, mu at the lagged column m-NO (for the dxz operands)
+    float lp0 = 0.f, lp1 = 0.f, mp0 = 1.f, mp1 = 1.f;
+
+    const int m0 = xs - 2 * NO + 1;            // first march column
+    const int m1 = xe + LAG;                    // last march column
+    // one-step-ahead fetches
+    float pux0, pux1, puz0, puz1, pl0, pl1, pm0, pm1, ql0, ql1, qm0, qm1;
+    load_u(m0, pux0, pux1, puz0, puz1);
+    load_mat(m0, pl0, pl1, pm0, pm1);
+    load_mat(m0 - NO + 1, ql0, ql1, qm0, qm1);
     {
-        float l0, l1, m0, m1;
-        load_mat(x0 + NO - 1, l0, l1, m0, m1);
-        RL1[0] = frcp(l0 + 2.0f * m0); RL1[1] = frcp(l1 + 2.0f * m1);
-        RM1[0] = frcp(m0); RM1[1] = frcp(m1);
+        float l0, l1, mm0, mm1;
+        load_mat(m0 - NO, l0, l1, mm0, mm1);
+        lp0 = l0; lp1 = l1; mp0 = mm0; mp1 = mm1;
+        rlp0 = frcp(l0 + 2.0f * mm0); rlp1 = frcp(l1 + 2.0f * mm1);
+        rmp0 = frcp(mm0); rmp1 = frcp(mm1);
     }
-#pragma unroll
-    for (int c = 0; c < WG; ++c) { Ga[c][0] = Ga[c][1] = Gb[c][0] = Gb[c][1] = 0.f; }
-#pragma unroll
-    for (int c = 0; c < WV; ++c) { V1[c][0] = V1[c][1] = V4[c][0] = V4[c][1] = 0.f; }
 
-    // the newest field and material columns are fetched one march step ahead of their use
-    float pux0, pux1, puz0, puz1, pl0, pl1, pm0, pm1;
-    load_u(x0 + 2 * NO - 1, pux0, pux1, puz0, puz1);
-    load_mat(x0 + NO, pl0, pl1, pm0, pm1);
-
-    for (int x = x0; x <= xe; ++x) {
-        // newest field column x+2NO-1, newest material column x+NO
-        Ux[W - 1][0] = pux0; Ux[W - 1][1] = pux1; Uz[W - 1][0] = puz0; Uz[W - 1][1] = puz1;
-        const float ln0 = pl0, ln1 = pl1, mn0 = pm0, mn1 = pm1;
-        load_u(x + 2 * NO, pux0, pux1, puz0, puz1);
-        load_mat(x + 1 + NO, pl0, pl1, pm0, pm1);
-        // operands of this column's update, issued before the arithmetic that hides their latency
-        float lc0 = 0.f, lc1 = 0.f, mc0 = 1.f, mc1 = 1.f;
-        float2 k2 = make_float2(0.f, 0.f), xp = k2, zp = k2;
-        const size_t ox = colbase(x);
-        if (x >= xs) {
-            load_mat(x, lc0, lc1, mc0, mc1);
+    for (int mc = m0; mc <= m1; ++mc) {
+        // this column's data (fetched last step) and the next column's fetches
+        const float ux0 = pux0, ux1 = pux1, uz0 = puz0, uz1 = puz1;
+        const float ln0 = pl0, ln1 = pl1, mn0 = pm0, mn1 = pm1;      // material at mc
+        const float lq0 = ql0, lq1 = ql1, mq0 = qm0, mq1 = qm1;      // material at mc-NO+1
+        load_u(mc + 1, pux0, pux1, puz0, puz1);
+        load_mat(mc + 1, pl0, pl1, pm0, pm1);
+        load_mat(mc + 2 - NO, ql0, ql1, qm0, qm1);
+        const int xc = mc - LAG;                 // cell completed this step
+        const bool emit = xc >= xs;
+        float2 k2 = make_float2(0.f, 0.f), xo = k2, zo = k2, xp = k2, zp = k2;
+        const int oc = colbase(xc);
+        if (emit) {
             if (store1) {
-                k2 = __ldg(reinterpret_cast<const float2*>(a.kdt2 + ox));
-                xp = *reinterpret_cast<const float2*>(uxn + ox);
-                zp = *reinterpret_cast<const float2*>(uzn + ox);
+                k2 = __ldg(reinterpret_cast<const float2*>(a.kdt2 + oc));
+                xo = __ldg(reinterpret_cast<const float2*>(uxc + oc));
+                zo = __ldg(reinterpret_cast<const float2*>(uzc + oc));
+                xp = *reinterpret_cast<const float2*>(uxn + oc);
+                zp = *reinterpret_cast<const float2*>(uzn + oc);
             } else if (store) {
-                k2.x = __ldg(a.kdt2 + ox);
-                xp.x = uxn[ox];
-                zp.x = uzn[ox];
+                k2.x = __ldg(a.kdt2 + oc);
+                xo.x = __ldg(uxc + oc);
+                zo.x = __ldg(uzc + oc);
+                xp.x = uxn[oc];
+                zp.x = uzn[oc];
             }
-        }
-        RL0[0] = RL1[0]; RL0[1] = RL1[1]; RM0[0] = RM1[0]; RM0[1] = RM1[1];
-        RL1[0] = frcp(ln0 + 2.0f * mn0); RL1[1] = frcp(ln1 + 2.0f * mn1);
-        RM1[0] = frcp(mn0); RM1[1] = frcp(mn1);
-
-        // staggered products at the half point x+NO-1/2 (window columns 2NO-1 | 2NO)
-        {
-            float sx0 = 0.f, sx1 = 0.f, sz0 = 0.f, sz1 = 0.f;
-#pragma unroll
-            for (int j = 1; j <= NO; ++j) {
-                const int cp = 2 * NO - 1 + j, cm = 2 * NO - j;
-                sx0 = fmaf(c_stag[NO][j], Ux[cp][0] - Ux[cm][0], sx0);
-                sx1 = fmaf(c_stag[NO][j], Ux[cp][1] - Ux[cm][1], sx1);
-                sz0 = fmaf(c_stag[NO][j], Uz[cp][0] - Uz[cm][0], sz0);
-                sz1 = fmaf(c_stag[NO][j], Uz[cp][1] - Uz[cm][1], sz1);
-            }
-            Ga[WG - 1][0] = 2.0f * frcp(RL0[0] + RL1[0]) * sx0;
-            Ga[WG - 1][1] = 2.0f * frcp(RL0[1] + RL1[1]) * sx1;
-            Gb[WG - 1][0] = 2.0f * frcp(RM0[0] + RM1[0]) * sz0;
-            Gb[WG - 1][1] = 2.0f * frcp(RM0[1] + RM1[1]) * sz1;
-        }
-        // dzx operands at column x+NO (window column 2NO)
-        {
-            float dzz0, dzz1, dzx0, dzx1;
-            dz_coll<NO>(Uz[2 * NO][0], Uz[2 * NO][1], dzz0, dzz1);
-            dz_coll<NO>(Ux[2 * NO][0], Ux[2 * NO][1], dzx0, dzx1);
-            V1[WV - 1][0] = ln0 * dzz0 * rdz; V1[WV - 1][1] = ln1 * dzz1 * rdz;
-            V4[WV - 1][0] = mn0 * dzx0 * rdz; V4[WV - 1][1] = mn1 * dzx1 * rdz;
         }
 
-        if (x >= xs) {
-            // dxz operands at column x: mu Dx uz / dx, lam Dx ux / dx
-            float s20 = 0.f, s21 = 0.f, s30 = 0.f, s31 = 0.f;
+        // --- x-staggered derivative: complete half point mc-NO+1/2, fold column mc into the chain
+        float sa0 = fmaf(c_stag[NO][NO], ux0, SA[0][0]), sa1 = fmaf(c_stag[NO][NO], ux1, SA[0][1]);
+        float sb0 = fmaf(c_stag[NO][NO], uz0, SB[0][0]), sb1 = fmaf(c_stag[NO][NO], uz1, SB[0][1]);
 #pragma unroll
-            for (int k = 1; k <= NO; ++k) {
-                s20 = fmaf(c_coll[NO][k], Uz[NO + k][0] - Uz[NO - k][0], s20);
-                s21 = fmaf(c_coll[NO][k], Uz[NO + k][1] - Uz[NO - k][1], s21);
-                s30 = fmaf(c_coll[NO][k], Ux[NO + k][0] - Ux[NO - k][0], s30);
-                s31 = fmaf(c_coll[NO][k], Ux[NO + k][1] - Ux[NO - k][1], s31);
+        for (int i = 0; i < NS - 1; ++i) {
+            // slot i+1 is the half point mc-NO+1/2+(i+1); column mc enters it with +c_{NO-i-1}
+            // (left of the point) or -c_{i+2-NO} (right of it)
+            const int ip = i + 1;
+            const float c = ip < NO ? c_stag[NO][NO - ip] : -c_stag[NO][ip - NO + 1];
+            SA[i][0] = fmaf(c, ux0, SA[ip][0]); SA[i][1] = fmaf(c, ux1, SA[ip][1]);
+            SB[i][0] = fmaf(c, uz0, SB[ip][0]); SB[i][1] = fmaf(c, uz1, SB[ip][1]);
+        }
+        SA[NS - 1][0] = 0.f; SA[NS - 1][1] = 0.f; SB[NS - 1][0] = 0.f; SB[NS - 1][1] = 0.f;
+
+        // harmonic means at the completed half point (columns mc-NO | mc-NO+1)
+        const float rlq0 = frcp(lq0 + 2.0f * mq0), rlq1 = frcp(lq1 + 2.0f * mq1);
+        const float rmq0 = frcp(mq0), rmq1 = frcp(mq1);
+        const float ga0 = 2.0f * frcp(rlp0 + rlq0) * sa0 * dx2, ga1 = 2.0f * frcp(rlp1 + rlq1) * sa1 * dx2;
+        const float gb0 = 2.0f * frcp(rmp0 + rmq0) * sb0 * dx2, gb1 = 2.0f * frcp(rmp1 + rmq1) * sb1 * dx2;
+
+        // --- x-collocated derivative: complete column mc-NO, fold column mc into the chain
+        const float d20 = fmaf(c_coll[NO][NO], uz0, D2[0][0]), d21 = fmaf(c_coll[NO][NO], uz1, D2[0][1]);
+        const float d30 = fmaf(c_coll[NO][NO], ux0, D3[0][0]), d31 = fmaf(c_coll[NO][NO], ux1, D3[0][1]);
+#pragma unroll
+        for (int j = 0; j < ND - 1; ++j) {
+            // slot j+1 is column mc-NO+j+1: column mc enters with +c1_{NO-j-1} (left), -c1_{j+1-NO} (right)
+            const int jp = j + 1;
+            if (jp == NO) {
+                D2[j][0] = D2[jp][0]; D2[j][1] = D2[jp][1];
+                D3[j][0] = D3[jp][0]; D3[j][1] = D3[jp][1];
+            } else {
+                const float c = jp < NO ? c_coll[NO][NO - jp] : -c_coll[NO][jp - NO];
+                D2[j][0] = fmaf(c, uz0, D2[jp][0]); D2[j][1] = fmaf(c, uz1, D2[jp][1]);
+                D3[j][0] = fmaf(c, ux0, D3[jp][0]); D3[j][1] = fmaf(c, ux1, D3[jp][1]);
             }
-            const float v20 = mc0 * s20 * rdx, v21 = mc1 * s21 * rdx;
-            const float v30 = lc0 * s30 * rdx, v31 = lc1 * s31 * rdx;
-            // z staggered products at column x below this lane's rows
-            float sa0, sa1, sb0, sb1;
-            dz_stag<NO>(Uz[NO][0], Uz[NO][1], sa0, sa1);
-            dz_stag<NO>(Ux[NO][0], Ux[NO][1], sb0, sb1);
-            const float rl0 = frcp(lc0 + 2.0f * mc0), rl1 = frcp(lc1 + 2.0f * mc1);
-            const float rm0 = frcp(mc0), rm1 = frcp(mc1);
+        }
+        D2[ND - 1][0] = 0.f; D2[ND - 1][1] = 0.f; D3[ND - 1][0] = 0.f; D3[ND - 1][1] = 0.f;
+
+        // --- z-direction terms of column mc (cell chain slot LAG)
+        float z2a0, z2a1, z2b0, z2b1;
+        {
+            float sza0, sza1, szb0, szb1;
+            dz_stag<NO>(uz0, uz1, sza0, sza1);
+            dz_stag<NO>(ux0, ux1, szb0, szb1);
+            const float rl0 = frcp(ln0 + 2.0f * mn0), rl1 = frcp(ln1 + 2.0f * mn1);
+            const float rm0 = frcp(mn0), rm1 = frcp(mn1);
             const float rl2 = zrow<2>(rl0, rl1), rm2 = zrow<2>(rm0, rm1);
-            const float gzA0 = 2.0f * frcp(rl0 + rl1) * sa0, gzA1 = 2.0f * frcp(rl1 + rl2) * sa1;
-            const float gzB0 = 2.0f * frcp(rm0 + rm1) * sb0, gzB1 = 2.0f * frcp(rm1 + rm2) * sb1;
-            float z2a0, z2a1, z2b0, z2b1, xzm0, xzm1, xzl0, xzl1;
-            dz_of_half<NO>(gzA0, gzA1, z2a0, z2a1);
-            dz_of_half<NO>(gzB0, gzB1, z2b0, z2b1);
-            dz_coll<NO>(v20, v21, xzm0, xzm1);
-            dz_coll<NO>(v30, v31, xzl0, xzl1);
+            const float gzA0 = 2.0f * frcp(rl0 + rl1) * sza0, gzA1 = 2.0f * frcp(rl1 + rl2) * sza1;
+            const float gzB0 = 2.0f * frcp(rm0 + rm1) * szb0, gzB1 = 2.0f * frcp(rm1 + rm2) * szb1;
+            dz_half<NO>(gzA0, gzA1, z2a0, z2a1);
+            dz_half<NO>(gzB0, gzB1, z2b0, z2b1);
+        }
+        // dzx operands of column mc: lam Dz uz / dz, mu Dz ux / dz
+        float v10, v11, v40, v41;
+        {
+            float t0, t1, s0, s1;
+            dz_coll<NO>(uz0, uz1, t0, t1);
+            dz_coll<NO>(ux0, ux1, s0, s1);
+            v10 = ln0 * t0 * rdz * rdx; v11 = ln1 * t1 * rdz * rdx;
+            v40 = mn0 * s0 * rdz * rdx; v41 = mn1 * s1 * rdz * rdx;
+        }
+        // dxz of column mc-NO: Dz(mu Dx uz / dx) / dz, Dz(lam Dx ux / dx) / dz
+        float xzm0, xzm1, xzl0, xzl1;
+        dz_coll<NO>(mp0 * d20 * rdx, mp1 * d21 * rdx, xzm0, xzm1);
+        dz_coll<NO>(lp0 * d30 * rdx, lp1 * d31 * rdx, xzl0, xzl1);
 
-            float x2a0 = 0.f, x2a1 = 0.f, x2b0 = 0.f, x2b1 = 0.f;
-            float zxl0 = 0.f, zxl1 = 0.f, zxm0 = 0.f, zxm1 = 0.f;
+        // --- fold everything into the force chain (slot i = cell mc-LAG+i) and advance it by one
+        // cell: slot 0 is complete and leaves the chain, slot i+1 moves to slot i (the move is the
+        // destination of the first fused multiply-add of that slot).
+        // staggered products at h = mc-NO+1/2 reach cells h -+ (k - 1/2): slots NO-k (+c_k), NO-1+k (-c_k)
+        // dzx operands of column mc reach cells mc -+ k: slots LAG-k (+c1_k), LAG+k (-c1_k)
+        float ex0 = 0.f, ex1 = 0.f, ez0 = 0.f, ez1 = 0.f;
+#pragma unroll
+        for (int i = 0; i < NF; ++i) {
+            float fx0 = FX[i][0], fx1 = FX[i][1], fz0 = FZ[i][0], fz1 = FZ[i][1];
 #pragma unroll
             for (int k = 1; k <= NO; ++k) {
-                const float cs = c_stag[NO][k], cc = c_coll[NO][k];
-                x2a0 = fmaf(cs, Ga[NO - 1 + k][0] - Ga[NO - k][0], x2a0);
-                x2a1 = fmaf(cs, Ga[NO - 1 + k][1] - Ga[NO - k][1], x2a1);
-                x2b0 = fmaf(cs, Gb[NO - 1 + k][0] - Gb[NO - k][0], x2b0);
-                x2b1 = fmaf(cs, Gb[NO - 1 + k][1] - Gb[NO - k][1], x2b1);
-                zxl0 = fmaf(cc, V1[NO + k][0] - V1[NO - k][0], zxl0);
-                zxl1 = fmaf(cc, V1[NO + k][1] - V1[NO - k][1], zxl1);
-                zxm0 = fmaf(cc, V4[NO + k][0] - V4[NO - k][0], zxm0);
-                zxm1 = fmaf(cc, V4[NO + k][1] - V4[NO - k][1], zxm1);
-            }
-            if (store) {
-                const float Fx0 = x2a0 * dx2 + zxl0 * rdx + z2b0 * dz2 + xzm0 * rdz;
-                const float Fx1 = x2a1 * dx2 + zxl1 * rdx + z2b1 * dz2 + xzm1 * rdz;
-                const float Fz0 = z2a0 * dz2 + xzl0 * rdz + x2b0 * dx2 + zxm0 * rdx;
-                const float Fz1 = z2a1 * dz2 + xzl1 * rdz + x2b1 * dx2 + zxm1 * rdx;
-                // own rows of an interior column carry no background: the window holds u^n
-                if (store1) {
-                    xp.x = fmaf(k2.x, Fx0, 2.0f * Ux[NO][0] - xp.x);
-                    xp.y = fmaf(k2.y, Fx1, 2.0f * Ux[NO][1] - xp.y);
-                    zp.x = fmaf(k2.x, Fz0, 2.0f * Uz[NO][0] - zp.x);
-                    zp.y = fmaf(k2.y, Fz1, 2.0f * Uz[NO][1] - zp.y);
-                    *reinterpret_cast<float2*>(uxn + ox) = xp;
-                    *reinterpret_cast<float2*>(uzn + ox) = zp;
-                } else {
-                    uxn[ox] = fmaf(k2.x, Fx0, 2.0f * Ux[NO][0] - xp.x);
-                    uzn[ox] = fmaf(k2.x, Fz0, 2.0f * Uz[NO][0] - zp.x);
+                if (i == NO - k) {
+                    fx0 = fmaf(c_stag[NO][k], ga0, fx0); fx1 = fmaf(c_stag[NO][k], ga1, fx1);
+                    fz0 = fmaf(c_stag[NO][k], gb0, fz0); fz1 = fmaf(c_stag[NO][k], gb1, fz1);
+                }
+                if (i == NO - 1 + k) {
+                    fx0 = fmaf(-c_stag[NO][k], ga0, fx0); fx1 = fmaf(-c_stag[NO][k], ga1, fx1);
+                    fz0 = fmaf(-c_stag[NO][k], gb0, fz0); fz1 = fmaf(-c_stag[NO][k], gb1, fz1);
+                }
+                if (i == LAG - k) {
+                    fx0 = fmaf(c_coll[NO][k], v10, fx0); fx1 = fmaf(c_coll[NO][k], v11, fx1);
+                    fz0 = fmaf(c_coll[NO][k], v40, fz0); fz1 = fmaf(c_coll[NO][k], v41, fz1);
+                }
+                if (i == LAG + k) {
+                    fx0 = fmaf(-c_coll[NO][k], v10, fx0); fx1 = fmaf(-c_coll[NO][k], v11, fx1);
+                    fz0 = fmaf(-c_coll[NO][k], v40, fz0); fz1 = fmaf(-c_coll[NO][k], v41, fz1);
                 }
             }
+            if (i == LAG) {   // z terms of column mc
+                fx0 = fmaf(z2b0, dz2, fx0); fx1 = fmaf(z2b1, dz2, fx1);
+                fz0 = fmaf(z2a0, dz2, fz0); fz1 = fmaf(z2a1, dz2, fz1);
+            }
+            if (i == NO - 1) {  // dxz of column mc-NO
+                fx0 = fmaf(xzm0, rdz, fx0); fx1 = fmaf(xzm1, rdz, fx1);
+                fz0 = fmaf(xzl0, rdz, fz0); fz1 = fmaf(xzl1, rdz, fz1);
+            }
+            if (i == 0) {
+                ex0 = fx0; ex1 = fx1; ez0 = fz0; ez1 = fz1;
+            } else {
+                FX[i - 1][0] = fx0; FX[i - 1][1] = fx1; FZ[i - 1][0] = fz0; FZ[i - 1][1] = fz1;
+            }
+        }
+        FX[NF - 1][0] = FX[NF - 1][1] = FZ[NF - 1][0] = FZ[NF - 1][1] = 0.f;
+
+        // cell xc is complete
+        if (emit && store) {
+            if (store1) {
+                xp.x = fmaf(k2.x, ex0, 2.0f * xo.x - xp.x);
+                xp.y = fmaf(k2.y, ex1, 2.0f * xo.y - xp.y);
+                zp.x = fmaf(k2.x, ez0, 2.0f * zo.x - zp.x);
+                zp.y = fmaf(k2.y, ez1, 2.0f * zo.y - zp.y);
+                *reinterpret_cast<float2*>(uxn + oc) = xp;
+                *reinterpret_cast<float2*>(uzn + oc) = zp;
+            } else {
+                uxn[oc] = fmaf(k2.x, ex0, 2.0f * xo.x - xp.x);
+                uzn[oc] = fmaf(k2.x, ez0, 2.0f * zo.x - zp.x);
+            }
         }
 
-        // slide the windows by one column
-#pragma unroll
-        for (int c = 0; c < W - 1; ++c) {
-            Ux[c][0] = Ux[c + 1][0]; Ux[c][1] = Ux[c + 1][1];
-            Uz[c][0] = Uz[c + 1][0]; Uz[c][1] = Uz[c + 1][1];
-        }
-#pragma unroll
-        for (int c = 0; c < WG - 1; ++c) {
-            Ga[c][0] = Ga[c + 1][0]; Ga[c][1] = Ga[c + 1][1];
-            Gb[c][0] = Gb[c + 1][0]; Gb[c][1] = Gb[c + 1][1];
-        }
-#pragma unroll
-        for (int c = 0; c < WV - 1; ++c) {
-            V1[c][0] = V1[c + 1][0]; V1[c][1] = V1[c + 1][1];
-            V4[c][0] = V4[c + 1][0]; V4[c][1] = V4[c + 1][1];
-        }
+        // lagged material: column mc-NO+1 becomes the left neighbour of the next half point
+        rlp0 = rlq0; rlp1 = rlq1; rmp0 = rmq0; rmp1 = rmq1;
+        lp0 = lq0; lp1 = lq1; mp0 = mq0; mp1 = mq1;
     }
 }
 

@@ -92,6 +92,17 @@ int fdfk_session_set_receivers(fdfk_session* s, int nrcv, const float* rx, const
  */
 int fdfk_session_advance(fdfk_session* s, int nsteps);
 
+/*
+ * fdfk_session_advance with a CUDA-event pair around every kernel launch (on
+ * the stream that launches it), then a synchronize: *ms_interior is the summed
+ * time of the interior fast-path kernel, *ms_edge that of the tiled kernel
+ * (top rows, absorbing layers, receivers).  Measurement only.
+ */
+int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, float* ms_edge);
+
+/* Cells per step handled by the interior fast path and by the tiled kernel. */
+int fdfk_session_interior_cells(const fdfk_session* s, long long* interior, long long* edge);
+
 /* Time index of the next step (0 after create). */
 int fdfk_session_step_index(const fdfk_session* s);
 
