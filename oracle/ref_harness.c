@@ -203,9 +203,43 @@ static int smooth(int n)
     return n == 1;
 }
 
+/* FFT / LU call log (observation only) */
+#define FLOG_MAX 4096
+typedef struct { int kind, n, sign; long off_in, off_out; } flog_t;
+static flog_t g_flog[FLOG_MAX];
+static int g_flog_n = 0, g_flog_on = 0;
+static double complex *g_fdata = NULL;
+static long g_fdata_len = 0, g_fdata_cap = 0;
+static long g_plan_calls = 0, g_exec_calls = 0, g_lu_calls = 0, g_lus_calls = 0;
+void fdfk_ref_flog(int on, long cap)
+{
+    g_flog_on = on; g_flog_n = 0; g_fdata_len = 0;
+    g_plan_calls = g_exec_calls = g_lu_calls = g_lus_calls = 0;
+    if (cap > g_fdata_cap) { free(g_fdata); g_fdata = (double complex *)malloc(sizeof(double complex) * cap); g_fdata_cap = cap; }
+}
+int fdfk_ref_flog_count(void) { return g_flog_n; }
+const flog_t *fdfk_ref_flog_get(int i) { return &g_flog[i]; }
+const double complex *fdfk_ref_flog_data(void) { return g_fdata; }
+void fdfk_ref_flog_counts(long *out) { out[0] = g_plan_calls; out[1] = g_exec_calls; out[2] = g_lu_calls; out[3] = g_lus_calls; }
+static void flog_add(int kind, int n, int sign, const double complex *in, const double complex *out, int nin, int nout)
+{
+    if (!g_flog_on) return;
+    int k = __atomic_fetch_add(&g_flog_n, 1, __ATOMIC_RELAXED);
+    if (k >= FLOG_MAX) return;
+    long need = nin + nout;
+    long off = __atomic_fetch_add(&g_fdata_len, need, __ATOMIC_RELAXED);
+    flog_t *r = &g_flog[k];
+    r->kind = kind; r->n = n; r->sign = sign; r->off_in = -1; r->off_out = -1;
+    if (off + need <= g_fdata_cap) {
+        if (nin) { memcpy(g_fdata + off, in, sizeof(double complex) * nin); r->off_in = off; }
+        if (nout) { memcpy(g_fdata + off + nin, out, sizeof(double complex) * nout); r->off_out = off + nin; }
+    }
+}
+
 void dfftw_plan_dft_1d_(int64_t *plan, const int *n, double complex *in, double complex *out, const int *sign,
                         const int *flags)
 {
+    if (g_flog_on) __atomic_fetch_add(&g_plan_calls, 1, __ATOMIC_RELAXED);
     (void)flags;
     fplan_t *p = (fplan_t *)calloc(1, sizeof(fplan_t));
     p->n = *n; p->sign = *sign; p->in = in; p->out = out;
@@ -266,13 +300,21 @@ static void plan_exec(const fplan_t *p, const double complex *x, double complex 
 void dfftw_execute_(const int64_t *plan)
 {
     const fplan_t *p = (const fplan_t *)(intptr_t)*plan;
+    double complex *tmp = g_flog_on ? (double complex *)malloc(sizeof(double complex) * p->n) : NULL;
+    if (tmp) memcpy(tmp, p->in, sizeof(double complex) * p->n);
     plan_exec(p, p->in, p->out);
+    if (g_flog_on) { __atomic_fetch_add(&g_exec_calls, 1, __ATOMIC_RELAXED); flog_add(1, p->n, p->sign, tmp, p->out, p->n, p->n); }
+    free(tmp);
 }
 
 void dfftw_execute_dft_(const int64_t *plan, double complex *in, double complex *out)
 {
     const fplan_t *p = (const fplan_t *)(intptr_t)*plan;
+    double complex *tmp = g_flog_on ? (double complex *)malloc(sizeof(double complex) * p->n) : NULL;
+    if (tmp) memcpy(tmp, in, sizeof(double complex) * p->n);
     plan_exec(p, in, out);
+    if (g_flog_on) { __atomic_fetch_add(&g_exec_calls, 1, __ATOMIC_RELAXED); flog_add(2, p->n, p->sign, tmp, out, p->n, p->n); }
+    free(tmp);
 }
 
 void dfftw_destroy_plan_(int64_t *plan)
@@ -292,6 +334,7 @@ static double cabs1(double complex z) { return fabs(creal(z)) + fabs(cimag(z)); 
 void zgetrf_(const int *m_, const int *n_, double complex *a, const int *lda_, int *ipiv, int *info)
 {
     int m = *m_, n = *n_, lda = *lda_;
+    if (g_flog_on) { __atomic_fetch_add(&g_lu_calls, 1, __ATOMIC_RELAXED); flog_add(3, n, m, a, NULL, lda * n, 0); }
     *info = 0;
     int mn = m < n ? m : n;
     for (int j = 0; j < mn; ++j) {
@@ -329,6 +372,7 @@ void zgetrs_(const char *trans, const int *n_, const int *nrhs_, const double co
     int n = *n_, nrhs = *nrhs_, lda = *lda_, ldb = *ldb_;
     *info = 0;
     char t = trans[0];
+    if (g_flog_on) { __atomic_fetch_add(&g_lus_calls, 1, __ATOMIC_RELAXED); flog_add(4, n, nrhs * 100 + (int)t, b, NULL, ldb * nrhs, 0); }
     for (int r = 0; r < nrhs; ++r) {
         double complex *x = b + (size_t)r * ldb;
         if (t == 'N' || t == 'n') {

@@ -14,6 +14,9 @@ Fixtures:
   shipped ``updatedispl_`` and ``loadseis`` restated from src/Submain.f90:33-116,
   with background strips from the shipped ``comput_background_wavefield_``
   (two-layer model, P incidence): FK inputs, strips, seismograms, final state.
+* ``fk_<name>.npz`` - one call of the shipped ``comput_background_wavefield_``
+  with different left and right layered models and back-azimuths that vary
+  along the profile: its inputs and the 12 background strips.
 """
 from __future__ import annotations
 
@@ -147,6 +150,25 @@ def loop_case():
     print("wrote loop_layered", "max|uz| %.3e" % np.abs(sz).max())
 
 
+FK_LEFT = np.array([[0.0, 2000.0], [6300.0, 8100.0], [3600.0, 4500.0], [2750.0, 3300.0]], np.float32)
+FK_RIGHT = np.array([[0.0, 900.0, 2600.0], [5500.0, 6300.0, 8100.0], [3200.0, 3600.0, 4500.0],
+                     [2600.0, 2750.0, 3300.0]], np.float32)
+
+
+def fk_case(name, src_type, rayp, baz_deg, f0, nt, dt, x0, z0, nx=16, nz=12, npml=6, nbd=3, dx=250.0, dz=200.0):
+    p = dict(nx=nx, nz=nz, npml=npml, izt=1, nbd=nbd, nt=nt, src_type=src_type, x0=x0, z0=z0, dx=dx, dz=dz,
+             dt=dt, ds=1e-3, f0=f0, rayp=rayp)
+    bazs = np.deg2rad(np.linspace(baz_deg[0], baz_deg[1], nx + 2 * npml))
+    fl = np.asfortranarray(FK_LEFT)
+    fr = np.asfortranarray(FK_RIGHT)
+    strips = {k: np.zeros(s, np.float32, order="F") for k, s in R.strip_shapes(nx, nz, nbd, nt).items()}
+    R.comput_background_wavefield(p, bazs, fl, fr, strips)
+    out = {"params": np.array([repr(p)]), "fk_left": fl, "fk_right": fr, "bazs": bazs}
+    out.update(strips)
+    np.savez_compressed(os.path.join(HERE, f"fk_{name}.npz"), **out)
+    print("wrote fk", name, "max %.3e" % max(np.abs(v).max() for v in strips.values()))
+
+
 if __name__ == "__main__":
     os.environ.setdefault("OMP_NUM_THREADS", "1")
     step_case("n3", 11, nx=30, nz=18, npml=12, norder=3)
@@ -155,3 +177,7 @@ if __name__ == "__main__":
     step_case("n3_minpml_aniso", 14, nx=20, nz=14, npml=5, norder=3, dx=250.0, dz=125.0)
     step_case("n2_odd", 15, nx=17, nz=11, npml=7, norder=2, dx=150.0, dz=175.0, dt=0.008)
     loop_case()
+    # P from the right (cos of the mean back-azimuth > 0), grid offset
+    fk_case("p_ramp", True, 0.07e-3, (-25.0, 20.0), 2.0, 120, 0.01, x0=-1500.0, z0=0.0)
+    # S from the left (cos < 0), low corner frequency, buried grid top
+    fk_case("s_left", False, 0.11e-3, (160.0, 200.0), 1.2, 110, 0.012, x0=500.0, z0=300.0)
