@@ -47,6 +47,27 @@ class Params(C.Structure):
                    float(p["dx"]), float(p["dz"]), float(p["dt"]), float(p["vpml"]), float(p.get("R0", 1e-3)))
 
 
+class FkParams(C.Structure):
+    """fdfk_fk_params: scalar arguments of comput_background_wavefield_ (src/FDFK2D.f90:429-431)."""
+    _fields_ = [("nx", C.c_int), ("nz", C.c_int), ("npml", C.c_int), ("izt", C.c_int), ("nbd", C.c_int),
+                ("nt", C.c_int), ("src_type", C.c_int), ("x0", C.c_float), ("z0", C.c_float), ("dx", C.c_float),
+                ("dz", C.c_float), ("dt", C.c_double), ("ds", C.c_float), ("f0", C.c_float), ("rayp", C.c_double)]
+
+    @classmethod
+    def from_dict(cls, p: dict) -> "FkParams":
+        return cls(int(p["nx"]), int(p["nz"]), int(p["npml"]), int(p.get("izt", 1)), int(p["nbd"]), int(p["nt"]),
+                   1 if p.get("src_type", True) else 0, float(p.get("x0", 0.0)), float(p.get("z0", 0.0)),
+                   float(p["dx"]), float(p["dz"]), float(p["dt"]), float(p["ds"]), float(p["f0"]),
+                   float(p["rayp"]))
+
+
+def _fk_model(m, name):
+    m = np.asfortranarray(m, np.float32)
+    if m.ndim != 2 or m.shape[0] != 4:
+        raise ValueError(f"{name} must have shape (4, nlayer): z_top, vp, vs, rho")
+    return m
+
+
 def lib_path() -> str:
     return os.path.join(PKG, "_build", "libfdfk_gb300.so")
 
@@ -70,7 +91,7 @@ def lib():
                      "fdfk_session_set_receivers", "fdfk_session_download_seismograms",
                      "fdfk_session_upload_state", "fdfk_session_download_state",
                      "fdfk_session_download_seismogram_range", "fdfk_session_advance_timed",
-                     "fdfk_session_interior_cells"):
+                     "fdfk_session_interior_cells", "fdfk_session_fk_background", "fdfk_fk_background"):
             getattr(L, name).restype = C.c_int if name != "fdfk_session_destroy" else None
         _lib = L
     return _lib
@@ -151,6 +172,17 @@ class Session:
         arr = (C.c_void_p * 12)(*[_f32(strips[k], k) for k in STRIPS])
         _check(lib().fdfk_session_upload_background(self._h, arr, C.c_int(t0), C.c_int(count)))
 
+    def fk_background(self, p: dict, bazs, fk_left, fk_right):
+        """Compute the FK background on the GPU straight into this session's strips (all times)."""
+        fl, fr = _fk_model(fk_left, "fk_left"), _fk_model(fk_right, "fk_right")
+        bz = np.ascontiguousarray(bazs, np.float64)
+        if bz.size != int(p["nx"]) + 2 * int(p["npml"]):
+            raise ValueError("bazs must hold nx + 2 npml back-azimuths")
+        prm = FkParams.from_dict(p)
+        _check(lib().fdfk_session_fk_background(self._h, C.byref(prm), bz.ctypes.data_as(C.c_void_p),
+                                                 C.c_int(fl.shape[1]), fl.ctypes.data_as(C.c_void_p),
+                                                 C.c_int(fr.shape[1]), fr.ctypes.data_as(C.c_void_p)))
+
     def set_receivers(self, rx, rz, x0: float, z0: float, nstp: int, nsis: int):
         rx = np.ascontiguousarray(rx, np.float32)
         rz = np.ascontiguousarray(rz, np.float32)
@@ -219,6 +251,43 @@ def simulate(p: dict, c: np.ndarray, strips: dict, rx, rz, x0: float, z0: float,
                            rz.ctypes.data_as(C.c_void_p), C.c_float(x0), C.c_float(z0), C.c_int(nstp),
                            C.c_int(nsis), _f32(sx, "seisx"), _f32(sz, "seisz")))
     return sx, sz
+
+
+def fk_background(p: dict, bazs, fk_left, fk_right) -> dict:
+    """comput_background_wavefield on the GPU: the 12 strips as Fortran-ordered float32 host arrays.
+
+    p: nx, nz, npml, nbd, nt, dt, dx, dz, x0, z0, ds, f0, rayp (s/m), src_type (True = P).
+    bazs: back-azimuths (rad) of the nx + 2 npml columns; fk_left / fk_right: (4, nlayer)
+    z_top, vp, vs, rho per layer, the last the half-space.
+    """
+    fl, fr = _fk_model(fk_left, "fk_left"), _fk_model(fk_right, "fk_right")
+    bz = np.ascontiguousarray(bazs, np.float64)
+    if bz.size != int(p["nx"]) + 2 * int(p["npml"]):
+        raise ValueError("bazs must hold nx + 2 npml back-azimuths")
+    out = {k: np.zeros(sh, np.float32, order="F")
+           for k, sh in strip_shapes(int(p["nx"]), int(p["nz"]), int(p["nbd"]), int(p["nt"])).items()}
+    arr = (C.c_void_p * 12)(*[_f32(out[k], k) for k in STRIPS])
+    prm = FkParams.from_dict(p)
+    _check(lib().fdfk_fk_background(C.byref(prm), bz.ctypes.data_as(C.c_void_p), C.c_int(fl.shape[1]),
+                                    fl.ctypes.data_as(C.c_void_p), C.c_int(fr.shape[1]),
+                                    fr.ctypes.data_as(C.c_void_p), arr))
+    return out
+
+
+def comput_background_wavefield(p: dict, bazs, fk_left, fk_right, strips: dict):
+    """The reference entry point comput_background_wavefield_ (32 arguments), on the GPU, in place."""
+    L = lib()
+    i = lambda v: C.byref(C.c_int(int(v)))
+    f = lambda v: C.byref(C.c_float(float(v)))
+    d = lambda v: C.byref(C.c_double(float(v)))
+    fl, fr = _fk_model(fk_left, "fk_left"), _fk_model(fk_right, "fk_right")
+    bz = np.ascontiguousarray(bazs, np.float64)
+    args = [i(p["nx"]), i(p["nz"]), i(p["npml"]), i(p.get("izt", 1)), i(p["nbd"]), i(p["nt"]), i(fl.shape[1]),
+            i(fr.shape[1]), i(1 if p.get("src_type", True) else 0), f(p.get("x0", 0.0)), f(p.get("z0", 0.0)),
+            f(p["dx"]), f(p["dz"]), d(p["dt"]), f(p["ds"]), f(p["f0"]), d(p["rayp"]),
+            bz.ctypes.data_as(C.c_void_p), fl.ctypes.data_as(C.c_void_p), fr.ctypes.data_as(C.c_void_p)]
+    args += [_f32(strips[k], k) for k in STRIPS]
+    L.comput_background_wavefield_(*args)
 
 
 def updatedispl(p: dict, strips: dict, c, coef0, coef1, ux, uz, bp: dict, bu: dict, it: int):

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libfdfk_gb300.so")
-SOURCES = ("fdfk_sweep.cu", "fdfk_capi.cu")
+SOURCES = ("fdfk_sweep.cu", "fdfk_capi.cu", "fdfk_fk.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -57,7 +57,7 @@ def build(verbose: bool = False, extra=()) -> str:
         for msg in ex.map(compile_one, zip(srcs, objs)):
             if verbose and msg:
                 print(msg, file=sys.stderr)
-    cmd = [cc, "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart"]
+    cmd = [cc, "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart", "-lcufft"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -1,5 +1,6 @@
 // C ABI of fdfk_gb300: sessions, the one-shot time loop and the gfortran-ABI
 // drop-in `updatedispl_`.  Declarations and contracts: include/fdfk_gb300.h.
+#include "fdfk_fk.cuh"
 #include "fdfk_gb300.h"
 #include "fdfk_sweep.cuh"
 
@@ -673,6 +674,108 @@ int fdfk_simulate(const fdfk_params* p, const float* c, const float* const strip
     }
     fdfk_session_destroy(s);
     return FDFK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FK background
+// ---------------------------------------------------------------------------
+static int fk_job(const fdfk_fk_params* p, const double* bazs, int nll, const float* fkl, int nlr,
+                  const float* fkr, FkJob& J)
+{
+    if (!p || !bazs || !fkl || !fkr) return fail(FDFK_EINVAL, "NULL argument");
+    if (p->izt != 1) return fail(FDFK_EUNSUPPORTED, "FK background: only izt = 1 (free surface on top) is implemented");
+    if (p->nx < 1 || p->nbd < 1 || p->nz <= p->nbd || p->npml < p->nbd || p->nt < 1 || !(p->dt > 0.0) ||
+        !(p->dx > 0.f) || !(p->dz > 0.f))
+        return fail(FDFK_EINVAL, "FK: need nx >= 1, nz > nbd >= 1, npml >= nbd, nt >= 1 and positive dt, dx, dz");
+    if (nll < 1 || nlr < 1 || nll > kFkMaxLayers || nlr > kFkMaxLayers)
+        return fail(FDFK_EINVAL, "FK: layer count must be 1.." + std::to_string(kFkMaxLayers));
+    J.nx = p->nx; J.nz = p->nz; J.npml = p->npml; J.nbd = p->nbd; J.nt = p->nt;
+    J.p_wave = p->src_type != 0;
+    J.x0 = p->x0; J.z0 = p->z0; J.dx = p->dx; J.dz = p->dz;
+    J.dt = p->dt; J.ds = p->ds; J.f0 = p->f0; J.rayp = p->rayp;
+    J.bazs = bazs;
+    J.nlayer[0] = nll; J.nlayer[1] = nlr;
+    J.model[0] = fkl; J.model[1] = fkr;
+    return FDFK_OK;
+}
+
+int fdfk_session_fk_background(fdfk_session* s, const fdfk_fk_params* p, const double* bazs, int nlayer_left,
+                               const float* fk_left, int nlayer_right, const float* fk_right)
+{
+    if (!s) return fail(FDFK_EINVAL, "session is NULL");
+    FkJob J{};
+    int rc = fk_job(p, bazs, nlayer_left, fk_left, nlayer_right, fk_right, J);
+    if (rc) return rc;
+    if (p->nx != s->p.nx || p->nz != s->p.nz || p->npml != s->p.npml || p->nbd != s->p.nbd || p->nt != s->p.nt)
+        return fail(FDFK_EINVAL, "FK geometry (nx, nz, npml, nbd, nt) differs from the session's");
+    std::string err;
+    long long nl = 0;
+    rc = fk_background(J, s->strip, s->stream, err, &nl);
+    g_launches += nl;
+    if (rc) return fail(rc, err);
+    for (int t = 0; t <= s->p.nt; ++t) s->have_bg[t] = 1;
+    return FDFK_OK;
+}
+
+int fdfk_fk_background(const fdfk_fk_params* p, const double* bazs, int nlayer_left, const float* fk_left,
+                       int nlayer_right, const float* fk_right, float* const strips[12])
+{
+    FkJob J{};
+    int rc = fk_job(p, bazs, nlayer_left, fk_left, nlayer_right, fk_right, J);
+    if (rc) return rc;
+    if (!strips) return fail(FDFK_EINVAL, "NULL strips");
+    for (int k = 0; k < NSTRIP; ++k)
+        if (!strips[k]) return fail(FDFK_EINVAL, "strip array is NULL");
+    float* d[NSTRIP] = {};
+    size_t bytes[NSTRIP];
+    auto release = [&]() {
+        for (int k = 0; k < NSTRIP; ++k) cudaFree(d[k]);
+    };
+    for (int k = 0; k < NSTRIP; ++k) {
+        bytes[k] = fk_strip_elems(p->nx, p->nz, p->nbd, k) * (size_t)(p->nt + 1) * sizeof(float);
+        if (cudaMalloc((void**)&d[k], bytes[k]) != cudaSuccess) {
+            release();
+            return fail(FDFK_ENOMEM, "FK: cudaMalloc of the strips failed");
+        }
+    }
+    std::string err;
+    long long nl = 0;
+    rc = fk_background(J, d, nullptr, err, &nl);
+    g_launches += nl;
+    if (rc) {
+        release();
+        return fail(rc, err);
+    }
+    for (int k = 0; k < NSTRIP; ++k) {
+        const cudaError_t e = cudaMemcpy(strips[k], d[k], bytes[k], cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            release();
+            return fail(FDFK_ECUDA, std::string("FK: copy of the strips failed: ") + cudaGetErrorString(e));
+        }
+    }
+    release();
+    return FDFK_OK;
+}
+
+void comput_background_wavefield_(const int* nx, const int* nz, const int* npml, const int* izt, const int* nbd,
+                                  const int* nt, const int* nlayer_left, const int* nlayer_right,
+                                  const int* src_type, const float* x0, const float* z0, const float* dx,
+                                  const float* dz, const double* dt, const float* ds, const float* f0,
+                                  const double* rayp, const double* bazs, const float* fk_left,
+                                  const float* fk_right, float* uxl_reg, float* uzl_reg, float* uxr_reg,
+                                  float* uzr_reg, float* uxb_reg, float* uzb_reg, float* uxl_pml, float* uzl_pml,
+                                  float* uxr_pml, float* uzr_pml, float* uxb_pml, float* uzb_pml)
+{
+    fdfk_fk_params p{};
+    p.nx = *nx; p.nz = *nz; p.npml = *npml; p.izt = *izt; p.nbd = *nbd; p.nt = *nt;
+    p.src_type = *src_type ? 1 : 0;
+    p.x0 = *x0; p.z0 = *z0; p.dx = *dx; p.dz = *dz; p.dt = *dt; p.ds = *ds; p.f0 = *f0; p.rayp = *rayp;
+    float* const strips[12] = {uxl_reg, uzl_reg, uxr_reg, uzr_reg, uxb_reg, uzb_reg,
+                               uxl_pml, uzl_pml, uxr_pml, uzr_pml, uxb_pml, uzb_pml};
+    if (fdfk_fk_background(&p, bazs, *nlayer_left, fk_left, *nlayer_right, fk_right, strips)) {
+        std::fprintf(stderr, "fdfk_gb300 comput_background_wavefield_: %s\n", g_err.c_str());
+        std::abort();
+    }
 }
 
 // ---------------------------------------------------------------------------

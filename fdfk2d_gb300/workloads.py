@@ -16,7 +16,9 @@ Density follows Gardner's rule rho = 1.74 Vp^0.25 g/cc with Vp in km/s
 :func:`plane_wave_background` fills the twelve background strips with an
 analytic P plane wave (Ricker wavelet) in the half-space below the model: a
 seeded stand-in for the FK background with the same shapes and value range,
-used where only the cost of the time loop matters.
+used where only the cost of the time loop matters.  :func:`fk_inputs` gives the
+arguments of the FK background (the 1-D models on either side) for the GPU
+FK path.
 """
 from __future__ import annotations
 
@@ -111,6 +113,7 @@ def config2(nt=12000, seed=2024):
     vs = vs * (1.0 + pert)
     w["c"] = pack_c(vp, vs)
     w["vp_half"] = 8100.0
+    w["fk_moho"] = (33e3, 50e3)
     p["vpml"] = float(vp.max())
     return w
 
@@ -169,6 +172,26 @@ def plane_wave_background(w, t0_index=0, count=None, out=None, amp=1e-3):
         else:
             res[name][...] = v
     return res
+
+
+def _fk_model(moho_m):
+    """Two-layer FK model (4, 2): z_top, vp, vs, rho (crust over mantle)."""
+    vp = np.array([6300.0, 8100.0])
+    return np.asfortranarray(np.stack([[0.0, moho_m], vp, [3600.0, 4500.0], gardner(vp)]).astype(np.float32))
+
+
+def fk_inputs(w, ds=1e-3):
+    """Arguments of comput_background_wavefield for a workload: (params, bazs, fk_left, fk_right).
+
+    config 1: the same crust (0-35 km) over mantle on both sides; config 2: crust 33 km thick on
+    the left, 50 km on the right.  The profile lies along the back-azimuth (bazs = 0).
+    """
+    p = w["p"]
+    fp = dict(nx=p["nx"], nz=p["nz"], npml=p["npml"], izt=1, nbd=p["nbd"], nt=p["nt"], src_type=True,
+              x0=w["x0"], z0=w["z0"], dx=p["dx"], dz=p["dz"], dt=p["dt"], ds=ds, f0=w["f0"], rayp=w["rayp"])
+    left, right = w.get("fk_moho", (35e3, 35e3))
+    bazs = np.zeros(p["nx"] + 2 * p["npml"])
+    return fp, bazs, _fk_model(left), _fk_model(right)
 
 
 def check_shapes(w, strips):

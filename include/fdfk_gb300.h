@@ -139,6 +139,54 @@ int fdfk_simulate(const fdfk_params* p, const float* c, const float* const strip
                   const float* rz, float x0, float z0, int nstp, int nsis, float* seisx, float* seisz);
 
 /*
+ * FK background wavefield (replaces lib_gnu/libFK3D.so's
+ * comput_background_wavefield_, called at src/FDFK2D.f90:429-431).
+ * Scalars of that call, same meaning and precision.
+ */
+typedef struct fdfk_fk_params {
+    int nx, nz, npml;
+    int izt;          /* 1 (free surface on top) is the implemented mode */
+    int nbd, nt;
+    int src_type;     /* reference logical: nonzero = incident P, 0 = incident SV */
+    float x0, z0, dx, dz;
+    double dt;
+    float ds, f0;     /* source scale and Ricker centre frequency */
+    double rayp;      /* ray parameter, s/m (the caller clamps |rayp| >= 1e-9) */
+} fdfk_fk_params;
+
+/*
+ * Computes the 12 background strips on the GPU (FP64 propagators, spectra
+ * and transforms; float32 strips) into host arrays in the reference layout.
+ * bazs: back-azimuths (rad) of columns 1-npml..nx+npml, profile frame
+ * (src/FDFK2D.f90:385-387).  fk_left / fk_right: (4, nlayer) column-major
+ * z_top, vp, vs, rho per layer, the last layer the half-space.
+ */
+int fdfk_fk_background(const fdfk_fk_params* p, const double* bazs, int nlayer_left, const float* fk_left,
+                       int nlayer_right, const float* fk_right, float* const strips[12]);
+
+/*
+ * Same computation written straight into the session's device-resident
+ * strips (all nt+1 time samples), with no host copy of the strips.  The FK
+ * geometry (nx, nz, npml, nbd, nt) must match the session's.
+ */
+int fdfk_session_fk_background(fdfk_session* s, const fdfk_fk_params* p, const double* bazs, int nlayer_left,
+                               const float* fk_left, int nlayer_right, const float* fk_right);
+
+/*
+ * Drop-in for lib_gnu/libFK3D.so's comput_background_wavefield_ (32
+ * arguments, gfortran ABI, by reference; call at src/FDFK2D.f90:429-431).
+ * Prints a message and aborts on failure, as a Fortran `stop` would.
+ */
+void comput_background_wavefield_(const int* nx, const int* nz, const int* npml, const int* izt, const int* nbd,
+                                  const int* nt, const int* nlayer_left, const int* nlayer_right,
+                                  const int* src_type, const float* x0, const float* z0, const float* dx,
+                                  const float* dz, const double* dt, const float* ds, const float* f0,
+                                  const double* rayp, const double* bazs, const float* fk_left,
+                                  const float* fk_right, float* uxl_reg, float* uzl_reg, float* uxr_reg,
+                                  float* uzr_reg, float* uxb_reg, float* uzb_reg, float* uxl_pml, float* uzl_pml,
+                                  float* uxr_pml, float* uzr_pml, float* uxb_pml, float* uzb_pml);
+
+/*
  * Drop-in for the shipped libHybrid.so + libPML.so entry point
  * `updatedispl_` (68 arguments, gfortran ABI, everything by reference),
  * called from src/FDFK2D.f90:516-522.  Each call uploads the state, runs one

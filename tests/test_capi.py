@@ -63,3 +63,22 @@ def test_shapes_match_reference_allocations():
     ps = F.pml_shapes(40, 24, 8)
     assert ps["bux1l"] == (2, 24, 8) and ps["bpxbx"] == (8, 56)
     assert len(F.BU) == 24 and F.BU[0] == "bux1l" and F.BU[12] == "bux1b" and F.BU[18] == "bux1t"
+
+
+def test_fk_entry_points_validate_without_gpu(built):
+    import fdfk2d_gb300 as F
+    p = dict(nx=16, nz=12, npml=6, nbd=3, nt=50, dt=0.01, dx=250.0, dz=250.0, ds=1e-3, f0=2.0, rayp=6e-5)
+    m = np.array([[0.0], [6000.0], [3500.0], [2700.0]], np.float32)
+    baz = np.zeros(16 + 12)
+    with pytest.raises(F.FDFKError) as e:
+        F.fk_background(dict(p, izt=2), baz, m, m)
+    assert e.value.code == -2
+    for change in (dict(nbd=7), dict(nz=3), dict(nt=0), dict(dt=0.0), dict(nx=0)):
+        with pytest.raises((F.FDFKError, ValueError)) as e:
+            F.fk_background(dict(p, **change), np.zeros(int(dict(p, **change)["nx"]) + 12), m, m)
+        if isinstance(e.value, F.FDFKError):
+            assert e.value.code == -1, change
+    with pytest.raises(ValueError):
+        F.fk_background(p, np.zeros(5), m, m)
+    with pytest.raises(ValueError):
+        F.fk_background(p, baz, m[:3], m)
