@@ -6,6 +6,12 @@ receiver sampling + the fused updatedispl_ step over the whole grid.  The
 workload is the 4001 x 2001 heterogeneous model (config 2: 400 x 200 km at
 100 m, 40-cell PML, FD order 6, 401 receivers) with seeded synthetic inputs.
 
+value: K steps with material and the FK background (computed on the GPU beforehand)
+resident in HBM.  e2e: one whole K-step solve through the C ABI from host buffers -
+session creation with the material copied from pinned memory, the FK background
+computed on the GPU from the host's 1-D models, K steps, seismograms copied back.
+fk_background: the FK background of the full workload (nt = 12000) alone.
+
 Prints one JSON line (rank 0).  Arms:
   default           the GPU path (this repository)
   --impl reference  the reference's CPU algorithm on this host's cores (the oracle
@@ -102,20 +108,6 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def pinned_strips(w, count, torch):
-    """Pinned host buffers (reference layout, time slowest) holding `count` steps of background."""
-    from fdfk2d_gb300.api import STRIPS, strip_shapes
-    p = w["p"]
-    shp = strip_shapes(p["nx"], p["nz"], p["nbd"], count - 1)
-    bufs, views = {}, {}
-    for k in STRIPS:
-        n1, n2, T = shp[k]
-        t = torch.empty((T, n2, n1), dtype=torch.float32, pin_memory=True)
-        bufs[k] = t
-        views[k] = t.numpy().transpose(2, 1, 0)   # Fortran (n1, n2, T) view
-    return bufs, views
-
-
 def cpu_reference(w, budget_s=15.0, max_steps=40):
     """The reference algorithm (oracle restatement) on the host cores over a bounded sample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -149,6 +141,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="config2", choices=["config2", "config1"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fk-full", action="store_true")
     args = ap.parse_args()
     K, Wm = args.steps, max(3, args.warmup)
 
@@ -162,7 +155,8 @@ def main():
     NZ, NX = p["nz"] + p["npml"], p["nx"] + 2 * p["npml"]
     cells = NZ * NX
     config = {"workload": w["name"], "grid": f"{NZ}x{NX} cells incl. PML", "fd_order": 2 * p["norder"],
-              "receivers": len(w["rx"]), "background": "analytic P plane wave on the FK strips (seeded stand-in)",
+              "receivers": len(w["rx"]),
+              "background": "FK background computed on the GPU (P, 0.07 s/km, 1 Hz; crust 33 / 50 km left / right)",
               "l2": "state 7 x 33 MB > 129 MB L2 (no flush needed)", "parallelism": f"replicas x{args.gpus}"}
 
     if args.impl == "reference":
@@ -188,24 +182,19 @@ def main():
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
 
-    # the loop's time axis for this benchmark: warm-up + timed (device-resident) + per-kernel timing
-    # + timed (end to end)
-    K2 = min(K, 200)
-    total = Wm + 2 * K + K2
-    q = dict(p, nt=total - 1)
-    wq = dict(w, p=q)
-    bufs, host = pinned_strips(wq, total, torch)
-    WL.plane_wave_background(wq, 0, total, out=host)
-    sess = F.Session(q, w["c"], stream=stream.cuda_stream)
-    sess.set_receivers(w["rx"], w["rz"], w["x0"], w["z0"], 1, total - 1)
-
     def barrier():
         torch.cuda.synchronize(dev)
         if world > 1:
             torch.distributed.barrier()
 
-    # ---- device-resident arm: inputs in HBM before the timed region
-    sess.upload_background(host, 0, Wm + K + K2)
+    # ---- device-resident arm: material and the FK background (computed on the GPU) in HBM
+    # before the timed region; time axis = warm-up + timed + per-kernel timing
+    K2 = min(K, 200)
+    q = dict(p, nt=Wm + K + K2 - 1)
+    fkp, bazs, fk_left, fk_right = WL.fk_inputs(dict(w, p=q))
+    sess = F.Session(q, w["c"], stream=stream.cuda_stream)
+    sess.fk_background(fkp, bazs, fk_left, fk_right)
+    sess.set_receivers(w["rx"], w["rz"], w["x0"], w["z0"], 1, q["nt"])
     sess.advance(Wm)
     sess.synchronize()
     clocks = ClockSampler(local)
@@ -231,23 +220,46 @@ def main():
     # ---- per-kernel durations (CUDA events on each kernel's own stream) for the roofline
     ms_int, ms_edge = sess.advance_timed(K2)
     cells_int, cells_edge = sess.cell_split()
+    sess.close()
 
-    # ---- end-to-end arm: host (pinned) background in, seismograms out, through the C ABI
-    t_e = Wm + K + K2
-    outx = np.zeros((K, len(w["rx"])), np.float32, order="F")
-    outz = np.zeros_like(outx, order="F")
+    # ---- end-to-end arm: one whole K-step solve through the C ABI from host buffers: material
+    # (pinned) and FK inputs in, FK background on the GPU, K steps, seismograms out
+    qe = dict(p, nt=K - 1)
+    fke, bazs_e, fl_e, fr_e = WL.fk_inputs(dict(w, p=qe))
+    c_pin = torch.empty((NX, NZ, 3), dtype=torch.float32, pin_memory=True)
+    c_host = c_pin.numpy().transpose(2, 1, 0)          # Fortran (3, NZ, NX) view
+    c_host[...] = w["c"]
     barrier()
     t0 = time.perf_counter()
-    sess.upload_background(host, t_e, K)
-    sess.advance(K)
-    sess.seismogram_range(t_e, K, outx, outz)
+    se = F.Session(qe, c_host, stream=stream.cuda_stream)
+    se.fk_background(fke, bazs_e, fl_e, fr_e)
+    se.set_receivers(w["rx"], w["rz"], w["x0"], w["z0"], 1, K - 1)
+    se.advance(K)
+    outx, outz = se.seismograms()
     barrier()
     t_e2e = time.perf_counter() - t0
+    se.close()
     e2e_value = cells * K * world / t_e2e / 1e6
-    h2d = sum(int(np.prod(host[k].shape[:2])) for k in F.STRIPS) * 4
-    d2h = len(w["rx"]) * 2 * 4
+    h2d = (c_host.nbytes + bazs_e.nbytes + fl_e.nbytes + fr_e.nbytes + 2 * 4 * len(w["rx"])) / K
+    d2h = (outx.nbytes + outz.nbytes) / K
     assert np.isfinite(outz).all()
-    sess.close()
+
+    # ---- FK background alone at the workload's full length (nt of the workload), device-resident
+    fk_ms = None
+    if rank == 0 and not args.no_fk_full:
+        sf = F.Session(p, w["c"], stream=stream.cuda_stream)
+        fkf, bazs_f, fl_f, fr_f = WL.fk_inputs(w)
+        sf.fk_background(fkf, bazs_f, fl_f, fr_f)          # warm-up (cuFFT plans, first touch)
+        barrier()
+        t0 = time.perf_counter()
+        sf.fk_background(fkf, bazs_f, fl_f, fr_f)
+        barrier()
+        fk_ms = (time.perf_counter() - t0) * 1e3
+        sf.close()
+        n_fft = 1
+        while n_fft < 2 * (p["nt"] + 1):
+            n_fft *= 2
+        series = sum(int(np.prod(s_[:2])) for s_ in F.strip_shapes(p["nx"], p["nz"], p["nbd"], p["nt"]).values())
 
     peak, peak_kind = measured_peak()
     # dominant kernel: the interior fast path (its own cells, its own event-timed duration)
@@ -266,8 +278,8 @@ def main():
         line = {"metric": METRIC, "value": round(value, 1), "unit": METRIC, "n_gpus": world, "steps": K, "warmup": Wm,
                 "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic", "config": config,
-                "e2e": {"value": round(e2e_value, 1), "unit": METRIC, "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": d2h},
+                "e2e": {"value": round(e2e_value, 1), "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(d2h)},
                 "gpu_launches": int(launches),
                 "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                              "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
@@ -277,6 +289,10 @@ def main():
                              "whole_step_equiv_gbs": round(step_equiv, 1),
                              "whole_step_frac": round(step_equiv / peak, 4)},
                 "cpu_baseline": cpu, "clocks": clk}
+        if fk_ms is not None:
+            line["fk_background"] = {"ms": round(fk_ms, 1), "nt": p["nt"], "series": series, "n_fft": n_fft,
+                                     "precision": "fp64 spectra and transforms, f32 strips",
+                                     "note": "whole FK background of the workload, device-resident output"}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
