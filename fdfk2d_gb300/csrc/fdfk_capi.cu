@@ -2,6 +2,7 @@
 // drop-in `updatedispl_`.  Declarations and contracts: include/fdfk_gb300.h.
 #include "fdfk_fk.cuh"
 #include "fdfk_gb300.h"
+#include "fdfk_noalloc.cuh"
 #include "fdfk_sweep.cuh"
 
 #include <cuda_runtime.h>
@@ -776,6 +777,40 @@ void comput_background_wavefield_(const int* nx, const int* nz, const int* npml,
         std::fprintf(stderr, "fdfk_gb300 comput_background_wavefield_: %s\n", g_err.c_str());
         std::abort();
     }
+}
+
+// ---------------------------------------------------------------------------
+// Single step on the static scratch (no allocation)
+// ---------------------------------------------------------------------------
+int fdfk_step_noalloc(const fdfk_params* p, int it, const float* const strips[12], const float* c, float* ux,
+                      float* uz, float* const bp[12], float* const bu[24], void* stream)
+{
+    int rc = validate(p);
+    if (rc) return rc;
+    if (!strips || !c || !ux || !uz || !bp || !bu) return fail(FDFK_EINVAL, "NULL argument");
+    for (int k = 0; k < NSTRIP; ++k)
+        if (!strips[k]) return fail(FDFK_EINVAL, "strip array is NULL");
+    for (int k = 0; k < 12; ++k)
+        if ((k < 4 || k >= 8) && !bp[k]) return fail(FDFK_EINVAL, "bp array is NULL");
+    for (int k = 0; k < 18; ++k)
+        if (!bu[k]) return fail(FDFK_EINVAL, "bu array is NULL");
+    if (it < 0 || it > p->nt) return fail(FDFK_EINVAL, "it outside 0..nt");
+    float stag[kMaxOrder + 1][kMaxOrder + 1], coll[kMaxOrder + 1][kMaxOrder + 1];
+    fd_tables(stag, coll);
+    std::string err;
+    long long nl = 0;
+    rc = step_noalloc(*p, it, strips, c, ux, uz, bp, bu, &stag[0][0], &coll[0][0], (cudaStream_t)stream, err, &nl);
+    g_launches += nl;
+    if (rc) return fail(rc, err);
+    return FDFK_OK;
+}
+
+long long fdfk_step_noalloc_capacity(void) { return (long long)kNoAllocFloats; }
+
+long long fdfk_step_noalloc_need(const fdfk_params* p)
+{
+    if (validate(p)) return -1;
+    return (long long)noalloc_floats_needed(*p);
 }
 
 // ---------------------------------------------------------------------------

@@ -187,6 +187,25 @@ void comput_background_wavefield_(const int* nx, const int* nz, const int* npml,
                                   float* uxr_pml, float* uzr_pml, float* uxb_pml, float* uzb_pml);
 
 /*
+ * One time step with updatedispl_'s meaning (same arrays, same in-place
+ * update of ux, uz, bp, bu; strips hold time samples 0..nt and sample `it`
+ * is used) that allocates nothing: no counterpart in the reference.  Every
+ * device buffer of the call is carved from one file-scope static device array
+ * of fdfk_step_noalloc_capacity() floats (16 Mi floats, 64 MiB); a geometry
+ * that needs more (fdfk_step_noalloc_need) is rejected with FDFK_EINVAL
+ * before any device work.  The call runs on `stream` (NULL: the default
+ * stream) and returns after that stream has drained.
+ * Races: the scratch is shared by every caller in the process on a device;
+ * calls that overlap in time (two host threads, or two streams) corrupt each
+ * other - serialise them.  The first call on a device resolves the scratch
+ * address (cudaGetSymbolAddress); make it before any stream capture begins.
+ */
+int fdfk_step_noalloc(const fdfk_params* p, int it, const float* const strips[12], const float* c, float* ux,
+                      float* uz, float* const bp[12], float* const bu[24], void* stream);
+long long fdfk_step_noalloc_capacity(void);
+long long fdfk_step_noalloc_need(const fdfk_params* p);
+
+/*
  * Drop-in for the shipped libHybrid.so + libPML.so entry point
  * `updatedispl_` (68 arguments, gfortran ABI, everything by reference),
  * called from src/FDFK2D.f90:516-522.  Each call uploads the state, runs one
