@@ -224,7 +224,8 @@ def main():
 
     # ---- end-to-end arm: one whole K-step solve through the C ABI from host buffers: material
     # (pinned) and FK inputs in, FK background on the GPU, K steps, seismograms out
-    qe = dict(p, nt=K - 1)
+    # (the FK damping alpha = 10 / (nt dt) needs a record of realistic length: at least 1000 samples)
+    qe = dict(p, nt=max(K - 1, 999))
     fke, bazs_e, fl_e, fr_e = WL.fk_inputs(dict(w, p=qe))
     c_pin = torch.empty((NX, NZ, 3), dtype=torch.float32, pin_memory=True)
     c_host = c_pin.numpy().transpose(2, 1, 0)          # Fortran (3, NZ, NX) view
@@ -233,9 +234,11 @@ def main():
     t0 = time.perf_counter()
     se = F.Session(qe, c_host, stream=stream.cuda_stream)
     se.fk_background(fke, bazs_e, fl_e, fr_e)
-    se.set_receivers(w["rx"], w["rz"], w["x0"], w["z0"], 1, K - 1)
+    se.set_receivers(w["rx"], w["rz"], w["x0"], w["z0"], 1, qe["nt"])
     se.advance(K)
-    outx, outz = se.seismograms()
+    outx = np.empty((K, len(w["rx"])), np.float32, order="F")
+    outz = np.empty_like(outx, order="F")
+    se.seismogram_range(0, K, outx, outz)
     barrier()
     t_e2e = time.perf_counter() - t0
     se.close()

@@ -20,7 +20,6 @@ cudaError_t launch_step(const StepArgs& a, cudaStream_t s);
 cudaError_t launch_march(const StepArgs& a, const MarchArgs& m, cudaStream_t s);
 int march_warp_slots(int norder);
 cudaError_t set_coefficients(const float* stag, const float* coll);
-size_t step_smem_bytes(int norder);
 }  // namespace fdfk
 
 using namespace fdfk;
@@ -238,6 +237,15 @@ int zero_state(fdfk_session* s)
     return FDFK_OK;
 }
 
+// The tiled kernel's share of a step: top band (when the fast path runs), absorbing layers and
+// receivers in one launch.
+cudaError_t launch_edge(const fdfk_session* s, const StepArgs& a, cudaStream_t st, int* launches)
+{
+    (void)s;
+    *launches = 1;
+    return launch_step(a, st);
+}
+
 }  // namespace
 
 extern "C" {
@@ -320,17 +328,28 @@ int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out
     s->march.z0 = 2 * p->norder + 1;
     s->march.band_out = 64 - 4 * p->norder;
     s->march.n_bands = march ? (p->nz - 2 * p->norder + s->march.band_out - 1) / s->march.band_out : 0;
-    // segments: one full wave of resident warps when the grid is large enough, else kMarchSeg columns
+    // segments: about two waves of resident warps, so that the hardware block scheduler evens out
+    // the per-SM progress, with 16..48 columns per segment (a segment re-primes its pipeline over
+    // 3*norder-1 columns)
     s->march.seg_len = kMarchSeg;
     s->march.n_segs = march ? (p->nx + kMarchSeg - 1) / kMarchSeg : 0;
     if (march) {
         const int slots = march_warp_slots(p->norder);
-        if (slots > 0 && s->march.n_bands * s->march.n_segs > slots) {
-            const int segs = slots / s->march.n_bands;
-            if (segs >= 1 && (p->nx + segs - 1) / segs <= 4 * kMarchSeg) {
-                s->march.n_segs = segs;
-                s->march.seg_len = (p->nx + segs - 1) / segs;
-                s->march.n_segs = (p->nx + s->march.seg_len - 1) / s->march.seg_len;
+        if (slots > 0) {
+            const long long work = (long long)p->nx * s->march.n_bands;
+            int len = (int)((work + 2LL * slots - 1) / (2LL * slots));
+            len = len < 16 ? 16 : len > 48 ? 48 : len;
+            // whole waves only: a few blocks left over would run alone at the end of the step
+            while (len < 48 && (long long)((p->nx + len - 1) / len) * s->march.n_bands > 2LL * slots) ++len;
+            s->march.seg_len = len;
+            s->march.n_segs = (p->nx + len - 1) / len;
+        }
+        // FDFK_MARCH_SEGLEN=<columns> overrides the segment length (tuning)
+        if (const char* sl = std::getenv("FDFK_MARCH_SEGLEN")) {
+            const int v = std::atoi(sl);
+            if (v >= 8) {
+                s->march.seg_len = v;
+                s->march.n_segs = (p->nx + v - 1) / v;
             }
         }
     }
@@ -343,13 +362,7 @@ int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out
             return fail(FDFK_ECUDA, "stream/event creation failed");
         }
     }
-    a.tiles_int_z = (a.int_rows + kTZ - 1) / kTZ;
-    a.tiles_int_x = (p->nx + kTX - 1) / kTX;
-    a.tiles_l_z = (p->nz + kTZ - 1) / kTZ;
-    a.tiles_l_x = (p->npml + kTX - 1) / kTX;
-    a.tiles_b_z = (p->npml + kTZ - 1) / kTZ;
-    a.tiles_b_x = (s->NX + kTX - 1) / kTX;
-    a.n_tiles = a.tiles_int_z * a.tiles_int_x + 2 * a.tiles_l_z * a.tiles_l_x + a.tiles_b_z * a.tiles_b_x;
+    plan_tiles(a, march);
     *out = s;
     return FDFK_OK;
 }
@@ -434,13 +447,14 @@ int fdfk_session_advance(fdfk_session* s, int nsteps)
             // PML, receivers) on a side stream next to the interior fast path.
             CK(cudaEventRecord(s->fork, s->stream));
             CK(cudaStreamWaitEvent(s->side, s->fork, 0));
-            cudaError_t e = launch_step(a, s->side);
+            int nl = 0;
+            cudaError_t e = launch_edge(s, a, s->side, &nl);
             if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("step launch: ") + cudaGetErrorString(e));
             e = launch_march(a, s->march, s->stream);
             if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("march launch: ") + cudaGetErrorString(e));
             CK(cudaEventRecord(s->join, s->side));
             CK(cudaStreamWaitEvent(s->stream, s->join, 0));
-            g_launches.fetch_add(2);
+            g_launches.fetch_add(nl + 1);
         } else {
             cudaError_t e = launch_step(a, s->stream);
             if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("step launch: ") + cudaGetErrorString(e));
@@ -487,7 +501,8 @@ int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, 
             cudaStreamWaitEvent(s->side, s->fork, 0);
         }
         cudaEventRecord(e[2], edge);
-        cudaError_t r = launch_step(a, edge);
+        int nl = 0;
+        cudaError_t r = launch_edge(s, a, edge, &nl);
         cudaEventRecord(e[3], edge);
         if (r == cudaSuccess && two) {
             cudaEventRecord(e[0], s->stream);
@@ -497,7 +512,7 @@ int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, 
             cudaStreamWaitEvent(s->stream, s->join, 0);
         }
         if (r != cudaSuccess) { cleanup(); return fail(FDFK_ECUDA, std::string("launch: ") + cudaGetErrorString(r)); }
-        g_launches.fetch_add(two ? 2 : 1);
+        g_launches.fetch_add(nl + (two ? 1 : 0));
         s->cur ^= 1;
         s->it += 1;
     }

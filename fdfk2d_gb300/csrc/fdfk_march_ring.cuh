@@ -1,0 +1,298 @@
+// The march of one warp, fed by asynchronous copies (included inside
+// namespace fdfk::march by fdfk_march.cuh).
+//
+// EX: the segment's columns (with the stencil reach) leave 1..nx (background
+// strips, PML columns, columns beyond the grid); EZ: the band passes row nz
+// (bottom strip rows, rows beyond the grid).  Values outside the grid are
+// written into the ring directly (u = 0, lambda = 0, mu = 1); the Omega_II
+// background is added to the register copies of u after the ring read, so the
+// ring keeps the raw u^n for the time update.
+// Each lane copies its own two rows of every field with cp.async into a
+// per-warp shared-memory ring, kAhead columns before they are used, so the
+// DRAM latency is covered by the march itself instead of by registers.
+//   ring A: ux, uz, lambda, mu of columns mc - (2NO-1) .. mc + kAhead (the
+//           newest column, the lagged material column mc-NO+1 and the
+//           emitted cell's u^n all come from here);
+//   ring B: dt^2/rho and u^{n-1} of the cell emitted kAhead columns later.
+// A lane only reads back what it copied itself, so cp.async.wait_group is the
+// only synchronisation (no barrier, no spin loop).
+
+template <int NO>
+struct Ring {
+    static constexpr int kAhead = 2;                            // columns fetched ahead of use
+    static constexpr int kNeedA = kAhead + 2 * NO;              // ring-A columns live at once
+    static constexpr int kSlotsA = kNeedA <= 4 ? 4 : kNeedA <= 8 ? 8 : 16;
+    static constexpr int kSlotsB = 4;                           // >= kAhead + 1
+    static constexpr int kFieldsA = 4;
+    static constexpr int kFieldsB = 3;
+    static constexpr int kWarpFloats = 64 * (kSlotsA * kFieldsA + kSlotsB * kFieldsB);
+};
+
+__device__ __forceinline__ void cp_async8(float* smem, const float* gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+__device__ __forceinline__ void st_shared2(float* smem, float v0, float v1)
+{
+    *reinterpret_cast<float2*>(smem) = make_float2(v0, v1);
+}
+
+template <int NO, bool EX, bool EZ>
+__device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m, int lane, int b, int xs, int xe,
+                                           float* ring)
+{
+    using RG = Ring<NO>;
+    constexpr int NS = 2 * NO;       // staggered partial sums
+    constexpr int ND = 2 * NO + 1;   // collocated partial sums
+    constexpr int NF = 3 * NO;       // force accumulators
+    constexpr int LAG = 2 * NO - 1;  // newest column minus completed cell
+
+    const int r0 = b + 2 * lane;
+    const int nx = a.nx, nz = a.nz, NZ = a.NZ, npml = a.npml, ldz = a.ldz, nbd = a.nbd, it = a.it;
+    const bool store = lane >= NO && lane <= 31 - NO && r0 >= m.z0 && r0 <= nz;
+    const bool store1 = store && (!EZ || r0 + 1 <= nz);
+    const bool rows_in = !EZ || (r0 >= 1 && r0 + 1 <= NZ);
+    const bool r0_in = r0 >= 1 && r0 <= NZ, r1_in = r0 + 1 >= 1 && r0 + 1 <= NZ;
+    const bool r1_int = !EZ || r0 + 1 <= nz;
+
+    const float* __restrict__ uxc = a.ux[a.cur];
+    const float* __restrict__ uzc = a.uz[a.cur];
+    float* __restrict__ uxn = a.ux[a.cur ^ 1];
+    float* __restrict__ uzn = a.uz[a.cur ^ 1];
+    const float rdx = 1.0f / a.dx, rdz = 1.0f / a.dz;
+    const float dx2 = a.dx2r, dz2 = a.dz2;
+
+    const int rowoff = r0 - 1;
+    auto gofs = [&](int ix) -> int { return (ix + npml - 1) * ldz + rowoff; };
+    float* const ringA = ring + 2 * lane;
+    float* const ringB = ring + 64 * RG::kSlotsA * RG::kFieldsA + 2 * lane;
+    auto slotA = [&](int col, int f) -> float* { return ringA + ((col & (RG::kSlotsA - 1)) * RG::kFieldsA + f) * 64; };
+    auto slotB = [&](int col, int f) -> float* { return ringB + ((col & (RG::kSlotsB - 1)) * RG::kFieldsB + f) * 64; };
+    auto rdA = [&](int col, int f) -> float2 { return *reinterpret_cast<const float2*>(slotA(col, f)); };
+    auto rdB = [&](int col, int f) -> float2 { return *reinterpret_cast<const float2*>(slotB(col, f)); };
+
+    const int m0 = xs - 2 * NO + 1;            // first march column
+    const int m1 = xe + LAG;                    // last march column
+    const int c0 = m0 - NO;                     // first column whose material is needed
+    // one commit group per column; ring B of column col holds the cell col - LAG
+    auto issue = [&](int col) {
+        if (col <= m1) {
+            if (EX && (col < 1 - npml || col > nx + npml)) {
+                st_shared2(slotA(col, 0), 0.f, 0.f);
+                st_shared2(slotA(col, 1), 0.f, 0.f);
+                st_shared2(slotA(col, 2), 0.f, 0.f);
+                st_shared2(slotA(col, 3), 1.f, 1.f);
+            } else {
+                const int o = gofs(col);
+                if (rows_in) {
+                    cp_async8(slotA(col, 0), uxc + o);
+                    cp_async8(slotA(col, 1), uzc + o);
+                    cp_async8(slotA(col, 2), a.lam + o);
+                    cp_async8(slotA(col, 3), a.mu + o);
+                } else {   // a lane straddling the bottom of the grid: rows outside read as u = lambda = 0, mu = 1
+                    st_shared2(slotA(col, 0), r0_in ? __ldg(uxc + o) : 0.f, r1_in ? __ldg(uxc + o + 1) : 0.f);
+                    st_shared2(slotA(col, 1), r0_in ? __ldg(uzc + o) : 0.f, r1_in ? __ldg(uzc + o + 1) : 0.f);
+                    st_shared2(slotA(col, 2), r0_in ? __ldg(a.lam + o) : 0.f, r1_in ? __ldg(a.lam + o + 1) : 0.f);
+                    st_shared2(slotA(col, 3), r0_in ? __ldg(a.mu + o) : 1.f, r1_in ? __ldg(a.mu + o + 1) : 1.f);
+                }
+            }
+            const int xcol = col - LAG;
+            if (store && xcol >= xs) {
+                const int oc = gofs(xcol);
+                if (store1) {
+                    cp_async8(slotB(col, 0), a.kdt2 + oc);
+                    cp_async8(slotB(col, 1), uxn + oc);
+                    cp_async8(slotB(col, 2), uzn + oc);
+                } else {
+                    st_shared2(slotB(col, 0), __ldg(a.kdt2 + oc), 0.f);
+                    st_shared2(slotB(col, 1), uxn[oc], 0.f);
+                    st_shared2(slotB(col, 2), uzn[oc], 0.f);
+                }
+            }
+        }
+        cp_commit();
+    };
+    // Omega_II background of column ix added to the register copy of u^n (columns outside 1..nx, rows below nz)
+    auto inject = [&](int ix, float& x0, float& x1, float& z0, float& z1) {
+        if (EX && ((ix <= 0 && ix >= 1 - nbd) || (ix > nx && ix <= nx + nbd)) && r0 <= nz) {
+            const bool left = ix <= 0;
+            const size_t so = (size_t)(r0 - 1) + (size_t)nz * ((size_t)(left ? ix - (1 - nbd) : ix - nx - 1) + (size_t)nbd * it);
+            const float* sx = a.strip[left ? UXL_PML : UXR_PML] + so;
+            const float* sz = a.strip[left ? UZL_PML : UZR_PML] + so;
+            x0 += __ldg(sx); z0 += __ldg(sz);
+            if (r1_int) { x1 += __ldg(sx + 1); z1 += __ldg(sz + 1); }
+        }
+        if (EZ && r0 + 1 > nz && ix >= 1 - nbd && ix <= nx + nbd) {
+            const size_t cb = (size_t)(nx + 2 * nbd) * it + (size_t)(ix - (1 - nbd));
+            if (r0 >= nz + 1 && r0 <= nz + nbd) {
+                const size_t so = (size_t)(r0 - nz - 1) + (size_t)nbd * cb;
+                x0 += __ldg(a.strip[UXB_PML] + so); z0 += __ldg(a.strip[UZB_PML] + so);
+            }
+            if (r0 + 1 >= nz + 1 && r0 + 1 <= nz + nbd) {
+                const size_t so = (size_t)(r0 - nz) + (size_t)nbd * cb;
+                x1 += __ldg(a.strip[UXB_PML] + so); z1 += __ldg(a.strip[UZB_PML] + so);
+            }
+        }
+    };
+    for (int c = c0; c < m0 + RG::kAhead; ++c) issue(c);
+    cp_wait<RG::kAhead>();                      // columns c0 .. m0-1 have landed
+
+    float SA[NS][2], SB[NS][2];
+    float D2[ND][2], D3[ND][2];
+    float FX[NF][2], FZ[NF][2];
+#pragma unroll
+    for (int i = 0; i < NS; ++i) SA[i][0] = SA[i][1] = SB[i][0] = SB[i][1] = 0.f;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) D2[i][0] = D2[i][1] = D3[i][0] = D3[i][1] = 0.f;
+#pragma unroll
+    for (int i = 0; i < NF; ++i) FX[i][0] = FX[i][1] = FZ[i][0] = FZ[i][1] = 0.f;
+
+    float lp0, lp1, mp0, mp1, rlp0, rlp1, rmp0, rmp1;
+    {
+        const float2 l = rdA(c0, 2), mm = rdA(c0, 3);
+        lp0 = l.x; lp1 = l.y; mp0 = mm.x; mp1 = mm.y;
+        rlp0 = frcp(lp0 + 2.0f * mp0); rlp1 = frcp(lp1 + 2.0f * mp1);
+        rmp0 = frcp(mp0); rmp1 = frcp(mp1);
+    }
+
+    for (int mc = m0; mc <= m1; ++mc) {
+        issue(mc + RG::kAhead);
+        cp_wait<RG::kAhead>();                  // column mc has landed
+        const float2 U = rdA(mc, 0), Z = rdA(mc, 1), LNv = rdA(mc, 2), MNv = rdA(mc, 3);
+        const float2 LQv = rdA(mc - NO + 1, 2), MQv = rdA(mc - NO + 1, 3);
+        float ux0 = U.x, ux1 = U.y, uz0 = Z.x, uz1 = Z.y;
+        if (EX || EZ) inject(mc, ux0, ux1, uz0, uz1);
+        const float ln0 = LNv.x, ln1 = LNv.y, mn0 = MNv.x, mn1 = MNv.y;
+        const float lq0 = LQv.x, lq1 = LQv.y, mq0 = MQv.x, mq1 = MQv.y;
+        const int xc = mc - LAG;
+        const bool emit = xc >= xs;
+
+        // --- x-staggered derivative
+        float sa0 = fmaf(c_stag[NO][NO], ux0, SA[0][0]), sa1 = fmaf(c_stag[NO][NO], ux1, SA[0][1]);
+        float sb0 = fmaf(c_stag[NO][NO], uz0, SB[0][0]), sb1 = fmaf(c_stag[NO][NO], uz1, SB[0][1]);
+#pragma unroll
+        for (int i = 0; i < NS - 1; ++i) {
+            const int ip = i + 1;
+            const float c = ip < NO ? c_stag[NO][NO - ip] : -c_stag[NO][ip - NO + 1];
+            SA[i][0] = fmaf(c, ux0, SA[ip][0]); SA[i][1] = fmaf(c, ux1, SA[ip][1]);
+            SB[i][0] = fmaf(c, uz0, SB[ip][0]); SB[i][1] = fmaf(c, uz1, SB[ip][1]);
+        }
+        SA[NS - 1][0] = 0.f; SA[NS - 1][1] = 0.f; SB[NS - 1][0] = 0.f; SB[NS - 1][1] = 0.f;
+
+        const float rlq0 = frcp(lq0 + 2.0f * mq0), rlq1 = frcp(lq1 + 2.0f * mq1);
+        const float rmq0 = frcp(mq0), rmq1 = frcp(mq1);
+        const float ga0 = 2.0f * frcp(rlp0 + rlq0) * sa0 * dx2, ga1 = 2.0f * frcp(rlp1 + rlq1) * sa1 * dx2;
+        const float gb0 = 2.0f * frcp(rmp0 + rmq0) * sb0 * dx2, gb1 = 2.0f * frcp(rmp1 + rmq1) * sb1 * dx2;
+
+        // --- x-collocated derivative
+        const float d20 = fmaf(c_coll[NO][NO], uz0, D2[0][0]), d21 = fmaf(c_coll[NO][NO], uz1, D2[0][1]);
+        const float d30 = fmaf(c_coll[NO][NO], ux0, D3[0][0]), d31 = fmaf(c_coll[NO][NO], ux1, D3[0][1]);
+#pragma unroll
+        for (int j = 0; j < ND - 1; ++j) {
+            const int jp = j + 1;
+            if (jp == NO) {
+                D2[j][0] = D2[jp][0]; D2[j][1] = D2[jp][1];
+                D3[j][0] = D3[jp][0]; D3[j][1] = D3[jp][1];
+            } else {
+                const float c = jp < NO ? c_coll[NO][NO - jp] : -c_coll[NO][jp - NO];
+                D2[j][0] = fmaf(c, uz0, D2[jp][0]); D2[j][1] = fmaf(c, uz1, D2[jp][1]);
+                D3[j][0] = fmaf(c, ux0, D3[jp][0]); D3[j][1] = fmaf(c, ux1, D3[jp][1]);
+            }
+        }
+        D2[ND - 1][0] = 0.f; D2[ND - 1][1] = 0.f; D3[ND - 1][0] = 0.f; D3[ND - 1][1] = 0.f;
+
+        // --- z-direction terms of column mc
+        float z2a0, z2a1, z2b0, z2b1;
+        {
+            float sza0, sza1, szb0, szb1;
+            dz_stag<NO>(uz0, uz1, sza0, sza1);
+            dz_stag<NO>(ux0, ux1, szb0, szb1);
+            const float rl0 = frcp(ln0 + 2.0f * mn0), rl1 = frcp(ln1 + 2.0f * mn1);
+            const float rm0 = frcp(mn0), rm1 = frcp(mn1);
+            const float rl2 = zrow<2>(rl0, rl1), rm2 = zrow<2>(rm0, rm1);
+            const float gzA0 = 2.0f * frcp(rl0 + rl1) * sza0, gzA1 = 2.0f * frcp(rl1 + rl2) * sza1;
+            const float gzB0 = 2.0f * frcp(rm0 + rm1) * szb0, gzB1 = 2.0f * frcp(rm1 + rm2) * szb1;
+            dz_half<NO>(gzA0, gzA1, z2a0, z2a1);
+            dz_half<NO>(gzB0, gzB1, z2b0, z2b1);
+        }
+        float v10, v11, v40, v41;
+        {
+            float t0, t1, s0, s1;
+            dz_coll<NO>(uz0, uz1, t0, t1);
+            dz_coll<NO>(ux0, ux1, s0, s1);
+            v10 = ln0 * t0 * rdz * rdx; v11 = ln1 * t1 * rdz * rdx;
+            v40 = mn0 * s0 * rdz * rdx; v41 = mn1 * s1 * rdz * rdx;
+        }
+        float xzm0, xzm1, xzl0, xzl1;
+        dz_coll<NO>(mp0 * d20 * rdx, mp1 * d21 * rdx, xzm0, xzm1);
+        dz_coll<NO>(lp0 * d30 * rdx, lp1 * d31 * rdx, xzl0, xzl1);
+
+        // --- force chain
+        float ex0 = 0.f, ex1 = 0.f, ez0 = 0.f, ez1 = 0.f;
+#pragma unroll
+        for (int i = 0; i < NF; ++i) {
+            float fx0 = FX[i][0], fx1 = FX[i][1], fz0 = FZ[i][0], fz1 = FZ[i][1];
+#pragma unroll
+            for (int k = 1; k <= NO; ++k) {
+                if (i == NO - k) {
+                    fx0 = fmaf(c_stag[NO][k], ga0, fx0); fx1 = fmaf(c_stag[NO][k], ga1, fx1);
+                    fz0 = fmaf(c_stag[NO][k], gb0, fz0); fz1 = fmaf(c_stag[NO][k], gb1, fz1);
+                }
+                if (i == NO - 1 + k) {
+                    fx0 = fmaf(-c_stag[NO][k], ga0, fx0); fx1 = fmaf(-c_stag[NO][k], ga1, fx1);
+                    fz0 = fmaf(-c_stag[NO][k], gb0, fz0); fz1 = fmaf(-c_stag[NO][k], gb1, fz1);
+                }
+                if (i == LAG - k) {
+                    fx0 = fmaf(c_coll[NO][k], v10, fx0); fx1 = fmaf(c_coll[NO][k], v11, fx1);
+                    fz0 = fmaf(c_coll[NO][k], v40, fz0); fz1 = fmaf(c_coll[NO][k], v41, fz1);
+                }
+                if (i == LAG + k) {
+                    fx0 = fmaf(-c_coll[NO][k], v10, fx0); fx1 = fmaf(-c_coll[NO][k], v11, fx1);
+                    fz0 = fmaf(-c_coll[NO][k], v40, fz0); fz1 = fmaf(-c_coll[NO][k], v41, fz1);
+                }
+            }
+            if (i == LAG) {
+                fx0 = fmaf(z2b0, dz2, fx0); fx1 = fmaf(z2b1, dz2, fx1);
+                fz0 = fmaf(z2a0, dz2, fz0); fz1 = fmaf(z2a1, dz2, fz1);
+            }
+            if (i == NO - 1) {
+                fx0 = fmaf(xzm0, rdz, fx0); fx1 = fmaf(xzm1, rdz, fx1);
+                fz0 = fmaf(xzl0, rdz, fz0); fz1 = fmaf(xzl1, rdz, fz1);
+            }
+            if (i == 0) {
+                ex0 = fx0; ex1 = fx1; ez0 = fz0; ez1 = fz1;
+            } else {
+                FX[i - 1][0] = fx0; FX[i - 1][1] = fx1; FZ[i - 1][0] = fz0; FZ[i - 1][1] = fz1;
+            }
+        }
+        FX[NF - 1][0] = FX[NF - 1][1] = FZ[NF - 1][0] = FZ[NF - 1][1] = 0.f;
+
+        // cell xc is complete
+        if (emit && store) {
+            const float2 k2 = rdB(mc, 0), xp = rdB(mc, 1), zp = rdB(mc, 2);
+            const float2 xo = rdA(xc, 0), zo = rdA(xc, 1);
+            float2 nxv, nzv;
+            nxv.x = fmaf(k2.x, ex0, 2.0f * xo.x - xp.x);
+            nxv.y = fmaf(k2.y, ex1, 2.0f * xo.y - xp.y);
+            nzv.x = fmaf(k2.x, ez0, 2.0f * zo.x - zp.x);
+            nzv.y = fmaf(k2.y, ez1, 2.0f * zo.y - zp.y);
+            const int oc = gofs(xc);
+            if (store1) {
+                *reinterpret_cast<float2*>(uxn + oc) = nxv;
+                *reinterpret_cast<float2*>(uzn + oc) = nzv;
+            } else {
+                uxn[oc] = nxv.x;
+                uzn[oc] = nzv.x;
+            }
+        }
+
+        rlp0 = rlq0; rlp1 = rlq1; rmp0 = rmq0; rmp1 = rmq1;
+        lp0 = lq0; lp1 = lq1; mp0 = mq0; mp1 = mq1;
+    }
+    cp_wait<0>();
+}

@@ -303,13 +303,7 @@ int step_noalloc(const fdfk_params& p, int it, const float* const strips[12], co
     a.dampx = dampx; a.dampz = dampz;
     for (int k = 0; k < NSTRIP; ++k) a.strip[k] = sp[k];   // time index `it` copied as sample 0
     a.int_rows = p.nz;                                      // the general tiled kernel for every row
-    a.tiles_int_z = (a.int_rows + kTZ - 1) / kTZ;
-    a.tiles_int_x = (p.nx + kTX - 1) / kTX;
-    a.tiles_l_z = (p.nz + kTZ - 1) / kTZ;
-    a.tiles_l_x = (p.npml + kTX - 1) / kTX;
-    a.tiles_b_z = (p.npml + kTZ - 1) / kTZ;
-    a.tiles_b_x = (NX + kTX - 1) / kTX;
-    a.n_tiles = a.tiles_int_z * a.tiles_int_x + 2 * a.tiles_l_z * a.tiles_l_x + a.tiles_b_z * a.tiles_b_x;
+    plan_tiles(a, false);
     a.ux[0] = ux0; a.ux[1] = ux1; a.uz[0] = uz0; a.uz[1] = uz1;
     for (int k = 0; k < 24; ++k) { a.bu[k][0] = bup[k][0]; a.bu[k][1] = bup[k][1]; }
     for (int k = 0; k < 12; ++k) a.bp[k] = bpp[k];

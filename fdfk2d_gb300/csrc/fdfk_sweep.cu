@@ -19,29 +19,41 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 namespace fdfk {
 
 __constant__ float c_stag[kMaxOrder + 1][kMaxOrder + 1];  // [n][j]: fd_coef0(j, n), zero for j > n
 __constant__ float c_coll[kMaxOrder + 1][kMaxOrder + 1];  // [n][j]: fd_coef1(j, n)
 
-template <int NO>
-struct Tile {
-    static constexpr int H = 2 * NO - 1;          // reach of dxx / dzz
-    static constexpr int UZ = kTZ + 2 * H;        // u tile (z fastest)
-    static constexpr int UX = kTX + 2 * H;
-    static constexpr int MZ = kTZ + 2 * NO;       // material tile
-    static constexpr int MX = kTX + 2 * NO;
-    static constexpr int XW = kTX + 2 * NO;       // x extent of x-consumed arrays
-    static constexpr int ZW = kTZ + 2 * NO;       // z extent of z-consumed arrays
-    static constexpr int U = UZ * UX;
-    static constexpr int M = MZ * MX;
-    static constexpr int AX = kTZ * XW;
-    static constexpr int AZ = ZW * kTX;
-    static constexpr int total = 2 * U + 5 * M + 4 * AX + 4 * AZ;
+// Shared-memory layout of a TZ x TX tile (z fastest) for stencil half-order NO.
+struct TileDims {
+    int TZ, TX;
+    int H;          // reach of dxx / dzz
+    int UZ, UX;     // u tile
+    int MZ, MX;     // material tile
+    int XW, ZW;     // extents of the x- / z-consumed arrays
+    int U, M, AX, AZ;
+    int total;      // floats
 };
+
+__host__ __device__ __forceinline__ TileDims tile_dims(int NO, int TZ, int TX)
+{
+    TileDims t;
+    t.TZ = TZ; t.TX = TX;
+    t.H = 2 * NO - 1;
+    t.UZ = TZ + 2 * t.H; t.UX = TX + 2 * t.H;
+    t.MZ = TZ + 2 * NO; t.MX = TX + 2 * NO;
+    t.XW = TX + 2 * NO; t.ZW = TZ + 2 * NO;
+    t.U = t.UZ * t.UX; t.M = t.MZ * t.MX;
+    t.AX = TZ * t.XW; t.AZ = t.ZW * TX;
+    t.total = 2 * t.U + 4 * t.M + 4 * t.AX + 4 * t.AZ;
+    return t;
+}
 
 struct Rect {
     int side;       // 0 interior, 1 left PML, 2 right PML, 3 bottom PML
+    int cls;        // tile class (StepArgs::tdz / tdx): 0 interior, 1 side PML, 2 bottom PML
     int z0, x0;     // first row / column of the tile
     int zlo, zhi, xlo, xhi;  // output rectangle (inclusive)
 };
@@ -115,7 +127,8 @@ __device__ __forceinline__ Rect decode_tile(const StepArgs& a, int b)
     int nl = a.tiles_l_z * a.tiles_l_x;
     if (b < ni) {
         r.side = 0;
-        r.z0 = 1 + (b % a.tiles_int_z) * kTZ; r.x0 = 1 + (b / a.tiles_int_z) * kTX;
+        r.cls = 0;
+        r.z0 = 1 + (b % a.tiles_int_z) * a.tdz[0]; r.x0 = 1 + (b / a.tiles_int_z) * a.tdx[0];
         r.zlo = 1; r.zhi = a.int_rows; r.xlo = 1; r.xhi = a.nx;
         return r;
     }
@@ -124,16 +137,18 @@ __device__ __forceinline__ Rect decode_tile(const StepArgs& a, int b)
         int right = b >= nl;
         if (right) b -= nl;
         r.side = right ? 2 : 1;
+        r.cls = 1;
         r.zlo = 1; r.zhi = a.nz;
         r.xlo = right ? a.nx + 1 : 1 - a.npml;
         r.xhi = right ? a.nx + a.npml : 0;
-        r.z0 = 1 + (b % a.tiles_l_z) * kTZ; r.x0 = r.xlo + (b / a.tiles_l_z) * kTX;
+        r.z0 = 1 + (b % a.tiles_l_z) * a.tdz[1]; r.x0 = r.xlo + (b / a.tiles_l_z) * a.tdx[1];
         return r;
     }
     b -= 2 * nl;
     r.side = 3;
+    r.cls = 2;
     r.zlo = a.nz + 1; r.zhi = a.nz + a.npml; r.xlo = 1 - a.npml; r.xhi = a.nx + a.npml;
-    r.z0 = r.zlo + (b % a.tiles_b_z) * kTZ; r.x0 = r.xlo + (b / a.tiles_b_z) * kTX;
+    r.z0 = r.zlo + (b % a.tiles_b_z) * a.tdz[2]; r.x0 = r.xlo + (b / a.tiles_b_z) * a.tdx[2];
     return r;
 }
 
@@ -181,44 +196,44 @@ __device__ void sample_receivers(const StepArgs& a, int blk)
 // The step kernel.
 // ---------------------------------------------------------------------------
 template <int NO>
-__global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
+__global__ void __launch_bounds__(kThreads, 3) fdfk_step_kernel(StepArgs a)
 {
-    using T = Tile<NO>;
-    constexpr int H = T::H;
+    constexpr int H = 2 * NO - 1;
     extern __shared__ float sm[];
     if ((int)blockIdx.x >= a.n_tiles) {
         sample_receivers(a, blockIdx.x - a.n_tiles);
         return;
     }
     const Rect R = decode_tile(a, blockIdx.x);
+    const TileDims T = tile_dims(NO, a.tdz[R.cls], a.tdx[R.cls]);
+    const int TZ = T.TZ, TX = T.TX;
     const bool pml = R.side != 0;
     const int tid = threadIdx.x;
     const int nx = a.nx, nz = a.nz, npml = a.npml;
     const int NZ = a.NZ;
 
     float* sux = sm;
-    float* suz = sux + T::U;
-    float* sLam = suz + T::U;
-    float* sMu = sLam + T::M;
-    float* sL2m = sMu + T::M;
-    float* sRL2m = sL2m + T::M;
-    float* sRMu = sRL2m + T::M;
-    float* gxA = sRMu + T::M;   // H(l2m) * Dstag_x(ux)   [label][z]
-    float* gxB = gxA + T::AX;   // H(mu)  * Dstag_x(uz)
-    float* v1 = gxB + T::AX;    // lam * Dz(uz)/dz        [x][z]  (dzx(lam uz))
-    float* v4 = v1 + T::AX;     // mu  * Dz(ux)/dz                 (dzx(mu ux))
-    float* gzA = v4 + T::AX;    // H(l2m) * Dstag_z(uz)   [x][label]
-    float* gzB = gzA + T::AZ;   // H(mu)  * Dstag_z(ux)
-    float* v2 = gzB + T::AZ;    // mu  * Dx(uz)/dx        [x][z]  (dxz(mu uz))
-    float* v3 = v2 + T::AZ;     // lam * Dx(ux)/dx                 (dxz(lam ux))
+    float* suz = sux + T.U;
+    float* sLam = suz + T.U;
+    float* sMu = sLam + T.M;
+    float* sRL2m = sMu + T.M;
+    float* sRMu = sRL2m + T.M;
+    float* gxA = sRMu + T.M;   // H(l2m) * Dstag_x(ux)   [label][z]
+    float* gxB = gxA + T.AX;   // H(mu)  * Dstag_x(uz)
+    float* v1 = gxB + T.AX;    // lam * Dz(uz)/dz        [x][z]  (dzx(lam uz))
+    float* v4 = v1 + T.AX;     // mu  * Dz(ux)/dz                 (dzx(mu ux))
+    float* gzA = v4 + T.AX;    // H(l2m) * Dstag_z(uz)   [x][label]
+    float* gzB = gzA + T.AZ;   // H(mu)  * Dstag_z(ux)
+    float* v2 = gzB + T.AZ;    // mu  * Dx(uz)/dx        [x][z]  (dxz(mu uz))
+    float* v3 = v2 + T.AZ;     // lam * Dx(ux)/dx                 (dxz(lam ux))
 
     const float rdx = 1.0f / a.dx, rdz = 1.0f / a.dz;
     const float* uxc = a.ux[a.cur];
     const float* uzc = a.uz[a.cur];
 
     // ---- phase 0: field tile (with injection) and material tile -------------
-    for (int i = tid; i < T::U; i += kThreads) {
-        int sz = i % T::UZ, sx = i / T::UZ;
+    for (int i = tid; i < T.U; i += kThreads) {
+        int sz = i % T.UZ, sx = i / T.UZ;
         int iz = R.z0 - H + sz, ix = R.x0 - H + sx;
         float vx = 0.f, vz = 0.f;
         if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
@@ -237,8 +252,8 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
         sux[i] = vx;
         suz[i] = vz;
     }
-    for (int i = tid; i < T::M; i += kThreads) {
-        int mz = i % T::MZ, mx = i / T::MZ;
+    for (int i = tid; i < T.M; i += kThreads) {
+        int mz = i % T.MZ, mx = i / T.MZ;
         int iz = R.z0 - NO + mz, ix = R.x0 - NO + mx;
         float l = 0.f, m = 1.f;
         if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
@@ -249,21 +264,20 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
         float l2 = l + 2.0f * m;
         sLam[i] = l;
         sMu[i] = m;
-        sL2m[i] = l2;
         sRL2m[i] = fast_rcp(l2);
         sRMu[i] = fast_rcp(m);
     }
     __syncthreads();
 
-#define SU(arr, z, x) arr[((x) + H) * T::UZ + ((z) + H)]
-#define SM(arr, z, x) arr[((x) + NO) * T::MZ + ((z) + NO)]
+#define SU(arr, z, x) arr[((x) + H) * T.UZ + ((z) + H)]
+#define SM(arr, z, x) arr[((x) + NO) * T.MZ + ((z) + NO)]
 
     // ---- phase 1a: x-direction staggered products and dzx operands -----------
-    for (int i = tid; i < T::AX; i += kThreads) {
-        int z = i % kTZ, xl = i / kTZ;
+    for (int i = tid; i < T.AX; i += kThreads) {
+        int z = i % TZ, xl = i / TZ;
         int iz = R.z0 + z;
         // staggered product at label L = xl - NO (half point between L and L+1)
-        if (xl < T::XW - 1) {
+        if (xl < T.XW - 1) {
             int L = xl - NO;
             int n = ordx(a, R.x0 + L, NO);
             float sx = 0.f, szv = 0.f;
@@ -298,10 +312,10 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
         }
     }
     // ---- phase 1b: z-direction staggered products and dxz operands -----------
-    for (int i = tid; i < T::AZ; i += kThreads) {
-        int zl = i % T::ZW, x = i / T::ZW;
+    for (int i = tid; i < T.AZ; i += kThreads) {
+        int zl = i % T.ZW, x = i / T.ZW;
         int ix = R.x0 + x;
-        if (zl < T::ZW - 1) {
+        if (zl < T.ZW - 1) {
             int L = zl - NO;
             int n = ordz(a, R.z0 + L, NO);
             float sz_ = 0.f, sx = 0.f;
@@ -336,18 +350,17 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
     }
     __syncthreads();
 
-#define GXI(arr, z, L) arr[((L) + NO) * kTZ + (z)]
-#define VXI(arr, z, x) arr[((x) + NO) * kTZ + (z)]
-#define GZI(arr, L, x) arr[(x) * T::ZW + ((L) + NO)]
-#define VZI(arr, z, x) arr[(x) * T::ZW + ((z) + NO)]
+#define GXI(arr, z, L) arr[((L) + NO) * TZ + (z)]
+#define VXI(arr, z, x) arr[((x) + NO) * TZ + (z)]
+#define GZI(arr, L, x) arr[(x) * T.ZW + ((L) + NO)]
+#define VZI(arr, z, x) arr[(x) * T.ZW + ((z) + NO)]
 
     // ---- phase 2: output cells ----------------------------------------------
-    const int z = tid % kTZ;
-    const int iz = R.z0 + z;
     const float dx = a.dx, dz = a.dz;
     const float dx2 = pml ? a.dx2p : a.dx2r;
-    for (int q = 0; q < kTX / (kThreads / kTZ); ++q) {
-        const int x = tid / kTZ + q * (kThreads / kTZ);
+    for (int cell = tid; cell < TZ * TX; cell += kThreads) {
+        const int z = cell % TZ, x = cell / TZ;
+        const int iz = R.z0 + z;
         const int ix = R.x0 + x;
         if (iz < R.zlo || iz > R.zhi || ix < R.xlo || ix > R.xhi) continue;
         const size_t g = gidx(a, iz, ix);
@@ -502,7 +515,7 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
             dzuz = fmaf(cz, SU(suz, z + k, x) - SU(suz, z - k, x), dzuz);
         }
         dxux /= dx; dxuz /= dx; dzux /= dz; dzuz /= dz;
-        const float lam0 = SM(sLam, z, x), mu0 = SM(sMu, z, x), l2m0 = SM(sL2m, z, x);
+        const float lam0 = SM(sLam, z, x), mu0 = SM(sMu, z, x), l2m0 = lam0 + 2.0f * mu0;
 
         const int base = side == 1 ? 0 : side == 2 ? 6 : 12;
         const int bpx0 = side == 1 ? 0 : side == 2 ? 2 : 8;
@@ -587,13 +600,16 @@ __global__ void __launch_bounds__(kThreads) fdfk_step_kernel(StepArgs a)
 template <int NO>
 static cudaError_t launch_no(const StepArgs& a, int n_sample_blocks, cudaStream_t s)
 {
-    size_t smem = sizeof(float) * (size_t)Tile<NO>::total;
-    static bool configured = false;
-    if (!configured) {
+    static int configured = 0;   // dynamic shared memory opted in so far (bytes)
+    size_t smem = 0;
+    for (int c = 0; c < 3; ++c)
+        smem = std::max(smem, sizeof(float) * (size_t)tile_dims(NO, a.tdz[c], a.tdx[c]).total);
+    if ((int)smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(fdfk_step_kernel<NO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        configured = true;
+        configured = (int)smem;
     }
+    if (a.n_tiles + n_sample_blocks == 0) return cudaSuccess;
     fdfk_step_kernel<NO><<<a.n_tiles + n_sample_blocks, kThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
@@ -614,19 +630,26 @@ cudaError_t launch_step(const StepArgs& a, cudaStream_t s)
     }
 }
 
-size_t step_smem_bytes(int norder)
+// Tile shapes and counts of the tiled kernel.  band_top: the fast path covers rows below
+// int_rows, so the interior tiles are flat kBandTZ x kBandTX tiles of the top band.  The
+// absorbing layers are cut into tiles whose thickness divides npml evenly (at most kPmlTile)
+// and kPmlRun cells along the layer.
+void plan_tiles(StepArgs& a, bool band_top)
 {
-    switch (norder) {
-    case 1: return sizeof(float) * Tile<1>::total;
-    case 2: return sizeof(float) * Tile<2>::total;
-    case 3: return sizeof(float) * Tile<3>::total;
-    case 4: return sizeof(float) * Tile<4>::total;
-    case 5: return sizeof(float) * Tile<5>::total;
-    case 6: return sizeof(float) * Tile<6>::total;
-    case 7: return sizeof(float) * Tile<7>::total;
-    case 8: return sizeof(float) * Tile<8>::total;
-    default: return 0;
-    }
+    auto cdiv = [](int x, int y) { return (x + y - 1) / y; };
+    const int nt = cdiv(a.npml, kPmlTile);
+    const int th = cdiv(a.npml, nt);
+    a.tdz[0] = band_top ? kBandTZ : kTZ;
+    a.tdx[0] = band_top ? kBandTX : kTX;
+    a.tdz[1] = kPmlRun; a.tdx[1] = th;
+    a.tdz[2] = th; a.tdx[2] = kPmlRun;
+    a.tiles_int_z = cdiv(a.int_rows, a.tdz[0]);
+    a.tiles_int_x = cdiv(a.nx, a.tdx[0]);
+    a.tiles_l_z = cdiv(a.nz, a.tdz[1]);
+    a.tiles_l_x = cdiv(a.npml, a.tdx[1]);
+    a.tiles_b_z = cdiv(a.npml, a.tdz[2]);
+    a.tiles_b_x = cdiv(a.NX, a.tdx[2]);
+    a.n_tiles = a.tiles_int_z * a.tiles_int_x + 2 * a.tiles_l_z * a.tiles_l_x + a.tiles_b_z * a.tiles_b_x;
 }
 
 cudaError_t set_coefficients(const float* stag, const float* coll)

@@ -14,8 +14,12 @@
 namespace fdfk {
 
 constexpr int kMaxOrder = 8;   // FD order 16 (the reference caps norder at (npml+1)/2)
-constexpr int kTZ = 32;        // tile rows (z, the contiguous axis)
-constexpr int kTX = 32;        // tile columns (x)
+constexpr int kTZ = 32;        // default tile rows (z, the contiguous axis)
+constexpr int kTX = 32;        // default tile columns (x)
+constexpr int kBandTZ = 8;     // flat tiles of the top band (rows 1..2*norder) next to the fast path
+constexpr int kBandTX = 64;
+constexpr int kPmlTile = 40;   // largest absorbing-layer thickness covered by one tile
+constexpr int kPmlRun = 24;    // absorbing-layer tile length along the layer
 constexpr int kThreads = 256;  // 8 warps per CTA
 
 // Strip order = argument order of updatedispl_ (src/FDFK2D.f90:517-518).
@@ -54,6 +58,7 @@ struct StepArgs {
     int tiles_l_z, tiles_l_x;           // left / right PML tiling (same shape)
     int tiles_b_z, tiles_b_x;           // bottom PML tiling
     int n_tiles;
+    int tdz[3], tdx[3];                 // tile rows / columns of the interior, side-PML and bottom-PML tiles
     // receivers sampled in the same launch (0 when this step takes no sample)
     int nrcv;
     int sample_index;          // istp
@@ -75,6 +80,9 @@ struct MarchArgs {
     int seg_len;     // columns per warp segment
     int n_segs;
 };
+
+// Tile shapes and counts of fdfk_step_kernel for a (fdfk_sweep.cu); needs nx, nz, npml, NX, int_rows.
+void plan_tiles(StepArgs& a, bool band_top);
 
 constexpr int kMarchSeg = 64;
 constexpr int kMarchMaxOrder = 4;
