@@ -86,12 +86,15 @@ def lib():
         L.fdfk_last_error.restype = C.c_char_p
         L.fdfk_kernel_launches.restype = C.c_longlong
         L.fdfk_session_create.argtypes = [C.POINTER(Params), C.c_void_p, C.POINTER(C.c_void_p)]
+        L.fdfk_batch_destroy.restype = None
         for name in ("fdfk_session_set_stream", "fdfk_session_advance", "fdfk_session_synchronize",
                      "fdfk_session_step_index", "fdfk_session_destroy", "fdfk_session_upload_background",
                      "fdfk_session_set_receivers", "fdfk_session_download_seismograms",
                      "fdfk_session_upload_state", "fdfk_session_download_state",
                      "fdfk_session_download_seismogram_range", "fdfk_session_advance_timed",
-                     "fdfk_session_interior_cells", "fdfk_session_fk_background", "fdfk_fk_background"):
+                     "fdfk_session_interior_cells", "fdfk_session_fk_background", "fdfk_fk_background",
+                     "fdfk_batch_create", "fdfk_batch_add", "fdfk_batch_remove", "fdfk_batch_set_graph_chunk",
+                     "fdfk_batch_advance", "fdfk_batch_synchronize", "fdfk_batch_live", "fdfk_batch_size"):
             getattr(L, name).restype = C.c_int if name != "fdfk_session_destroy" else None
         _lib = L
     return _lib
@@ -236,6 +239,58 @@ class Session:
         bpp = (C.c_void_p * 12)(*[_f32(bp[k], k) if k in bp else None for k in BP])
         bup = (C.c_void_p * 24)(*[_f32(bu[k], k) if k in bu else None for k in BU])
         _check(lib().fdfk_session_download_state(self._h, _f32(ux, "ux"), _f32(uz, "uz"), bpp, bup))
+
+
+class Batch:
+    """Solves (Sessions of one stencil order) advanced together: three launches per step for all
+    members, chunks of steps replayed from a captured CUDA graph."""
+
+    def __init__(self, norder: int, graph_chunk: int | None = None):
+        L = lib()
+        h = C.c_void_p()
+        _check(L.fdfk_batch_create(C.c_int(int(norder)), C.byref(h)))
+        self._h = h
+        self.members = []
+        if graph_chunk is not None:
+            _check(L.fdfk_batch_set_graph_chunk(self._h, C.c_int(int(graph_chunk))))
+
+    def add(self, session: "Session"):
+        _check(lib().fdfk_batch_add(self._h, session._h))
+        self.members.append(session)
+
+    def remove(self, session: "Session"):
+        _check(lib().fdfk_batch_remove(self._h, session._h))
+        self.members.remove(session)
+
+    def advance(self, nsteps: int):
+        _check(lib().fdfk_batch_advance(self._h, C.c_int(int(nsteps))))
+
+    def synchronize(self):
+        _check(lib().fdfk_batch_synchronize(self._h))
+
+    def live(self) -> int:
+        n = lib().fdfk_batch_live(self._h)
+        if n < 0:
+            _check(n)
+        return int(n)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fdfk_batch_destroy(self._h)
+            self._h = None
+            self.members = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def simulate(p: dict, c: np.ndarray, strips: dict, rx, rz, x0: float, z0: float, nstp: int, nsis: int):

@@ -3,6 +3,7 @@
 #include "fdfk_fk.cuh"
 #include "fdfk_gb300.h"
 #include "fdfk_noalloc.cuh"
+#include "fdfk_session.h"
 #include "fdfk_sweep.cuh"
 
 #include <cuda_runtime.h>
@@ -34,6 +35,15 @@ int fail(int code, const std::string& msg)
     g_err = msg;
     return code;
 }
+
+}  // namespace
+
+namespace fdfk {
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+void count_launches(long long n) { g_launches += n; }
+}  // namespace fdfk
+
+namespace {
 
 #define CK(call)                                                                                     \
     do {                                                                                             \
@@ -99,36 +109,6 @@ size_t bp_elems(const fdfk_params& p, int k)
 }
 
 }  // namespace
-
-struct fdfk_session {
-    fdfk_params p{};
-    int NZ = 0, NX = 0, ldz = 0;
-    cudaStream_t stream = nullptr;
-    cudaStream_t side = nullptr;     // second stream for the tiled kernel
-    cudaEvent_t fork = nullptr, join = nullptr;
-    float* kdt2 = nullptr;
-    float* lam = nullptr;
-    float* mu = nullptr;
-    float* ux[2] = {nullptr, nullptr};
-    float* uz[2] = {nullptr, nullptr};
-    float* bu[24][2] = {};
-    float* bp[12] = {};
-    DampCol* dampx = nullptr;
-    DampCol* dampz = nullptr;
-    float* strip[NSTRIP] = {};
-    std::vector<char> have_bg;   // per time index
-    int cur = 0;
-    int it = 0;
-    // receivers
-    int nrcv = 0, nstp = 1, nsis = -1, isis = 0, istp = 0;
-    float x0 = 0.f, z0 = 0.f;
-    float* rx = nullptr;
-    float* rz = nullptr;
-    float* seisx = nullptr;
-    float* seisz = nullptr;
-    StepArgs base{};
-    MarchArgs march{};
-};
 
 namespace {
 
@@ -376,6 +356,7 @@ int fdfk_session_set_stream(fdfk_session* s, void* stream)
 
 int fdfk_session_upload_background(fdfk_session* s, const float* const strips[12], int t0, int count)
 {
+    if (s && s->batch) return fail(FDFK_ESTATE, "the session is a member of a batch");
     if (!s || !strips) return fail(FDFK_EINVAL, "NULL argument");
     if (t0 < 0 || count < 0 || t0 + count > s->p.nt + 1) return fail(FDFK_EINVAL, "time range outside 0..nt");
     for (int k = 0; k < NSTRIP; ++k) {
@@ -391,6 +372,7 @@ int fdfk_session_upload_background(fdfk_session* s, const float* const strips[12
 int fdfk_session_set_receivers(fdfk_session* s, int nrcv, const float* rx, const float* rz, float x0, float z0,
                                int nstp, int nsis)
 {
+    if (s && s->batch) return fail(FDFK_ESTATE, "the session is a member of a batch");
     if (!s) return fail(FDFK_EINVAL, "session is NULL");
     if (nrcv < 0 || (nrcv > 0 && (!rx || !rz)) || nstp < 1 || nsis < 0) return fail(FDFK_EINVAL, "bad receiver arguments");
     const float xmax = x0 + (s->p.nx - 1) * s->p.dx, zmax = z0 + (s->p.nz - 1) * s->p.dz;
@@ -420,6 +402,7 @@ int fdfk_session_set_receivers(fdfk_session* s, int nrcv, const float* rx, const
 int fdfk_session_advance(fdfk_session* s, int nsteps)
 {
     if (!s) return fail(FDFK_EINVAL, "session is NULL");
+    if (s->batch) return fail(FDFK_ESTATE, "the session is a member of a batch; advance the batch");
     if (nsteps < 0) return fail(FDFK_EINVAL, "nsteps must be >= 0");
     if (s->it + nsteps > s->p.nt + 1) return fail(FDFK_EINVAL, "advance past the last time index nt");
     for (int k = 0; k < nsteps; ++k) {
@@ -469,6 +452,7 @@ int fdfk_session_advance(fdfk_session* s, int nsteps)
 int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, float* ms_edge)
 {
     if (!s || !ms_interior || !ms_edge) return fail(FDFK_EINVAL, "NULL argument");
+    if (s->batch) return fail(FDFK_ESTATE, "the session is a member of a batch; advance the batch");
     *ms_interior = 0.f;
     *ms_edge = 0.f;
     if (nsteps <= 0) return fdfk_session_advance(s, nsteps);
@@ -542,6 +526,10 @@ int fdfk_session_step_index(const fdfk_session* s) { return s ? s->it : FDFK_EIN
 
 int fdfk_session_synchronize(fdfk_session* s)
 {
+    if (s && s->batch) {
+        const int rb = fdfk_batch_synchronize(s->batch);
+        if (rb) return rb;
+    }
     if (!s) return fail(FDFK_EINVAL, "session is NULL");
     CK(cudaStreamSynchronize(s->stream));
     return FDFK_OK;
@@ -549,6 +537,10 @@ int fdfk_session_synchronize(fdfk_session* s)
 
 int fdfk_session_download_seismograms(fdfk_session* s, float* seisx, float* seisz)
 {
+    if (s && s->batch) {
+        const int rb = fdfk_batch_synchronize(s->batch);
+        if (rb) return rb;
+    }
     if (!s || !seisx || !seisz) return fail(FDFK_EINVAL, "NULL argument");
     if (s->nrcv == 0) return FDFK_OK;
     const size_t ns = (size_t)(s->nsis + 1) * s->nrcv;
@@ -560,6 +552,10 @@ int fdfk_session_download_seismograms(fdfk_session* s, float* seisx, float* seis
 
 int fdfk_session_download_seismogram_range(fdfk_session* s, int first, int count, float* seisx, float* seisz)
 {
+    if (s && s->batch) {
+        const int rb = fdfk_batch_synchronize(s->batch);
+        if (rb) return rb;
+    }
     if (!s || !seisx || !seisz) return fail(FDFK_EINVAL, "NULL argument");
     if (first < 0 || count < 0 || first + count > s->nsis + 1) return fail(FDFK_EINVAL, "sample range outside 0..nsis");
     if (s->nrcv == 0 || count == 0) return FDFK_OK;
@@ -575,6 +571,7 @@ int fdfk_session_download_seismogram_range(fdfk_session* s, int first, int count
 int fdfk_session_upload_state(fdfk_session* s, const float* ux, const float* uz, const float* const bp[12],
                               const float* const bu[24], int it)
 {
+    if (s && s->batch) return fail(FDFK_ESTATE, "the session is a member of a batch");
     if (!s || !ux || !uz || !bp || !bu) return fail(FDFK_EINVAL, "NULL argument");
     if (it < 0 || it > s->p.nt + 1) return fail(FDFK_EINVAL, "it outside 0..nt+1");
     const size_t n = (size_t)s->ldz * s->NX;
@@ -616,6 +613,10 @@ int fdfk_session_upload_state(fdfk_session* s, const float* ux, const float* uz,
 
 int fdfk_session_download_state(fdfk_session* s, float* ux, float* uz, float* const bp[12], float* const bu[24])
 {
+    if (s && s->batch) {
+        const int rb = fdfk_batch_synchronize(s->batch);
+        if (rb) return rb;
+    }
     if (!s || !ux || !uz || !bp || !bu) return fail(FDFK_EINVAL, "NULL argument");
     const size_t n = (size_t)s->ldz * s->NX;
     std::vector<float> lv[4];
@@ -671,6 +672,7 @@ int fdfk_session_download_state(fdfk_session* s, float* ux, float* uz, float* co
 
 void fdfk_session_destroy(fdfk_session* s)
 {
+    if (s && s->batch) fdfk_batch_remove(s->batch, s);
     if (s && s->stream) cudaStreamSynchronize(s->stream);
     free_session(s);
 }
@@ -718,6 +720,7 @@ static int fk_job(const fdfk_fk_params* p, const double* bazs, int nll, const fl
 int fdfk_session_fk_background(fdfk_session* s, const fdfk_fk_params* p, const double* bazs, int nlayer_left,
                                const float* fk_left, int nlayer_right, const float* fk_right)
 {
+    if (s && s->batch) return fail(FDFK_ESTATE, "the session is a member of a batch");
     if (!s) return fail(FDFK_EINVAL, "session is NULL");
     FkJob J{};
     int rc = fk_job(p, bazs, nlayer_left, fk_left, nlayer_right, fk_right, J);

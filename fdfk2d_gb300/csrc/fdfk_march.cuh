@@ -129,13 +129,13 @@ namespace march {
 
 }  // namespace march
 
+// Warp `warp` of one solve's fast-path launch.
 template <int NO>
-__global__ void __launch_bounds__(128) fdfk_march_kernel(StepArgs a, MarchArgs m)
+__device__ __forceinline__ void march_warp(const StepArgs& a, const MarchArgs& m, int warp)
 {
     extern __shared__ float ring_smem[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    const int warp = (blockIdx.x * (blockDim.x >> 5)) + wib;
     if (warp >= m.n_bands * m.n_segs) return;
     const int band = warp % m.n_bands, seg = warp / m.n_bands;
     const int b = m.z0 + band * m.band_out - 2 * NO;   // first row of the band
@@ -153,6 +153,21 @@ __global__ void __launch_bounds__(128) fdfk_march_kernel(StepArgs a, MarchArgs m
         if (ez) march::march_ring<NO, false, true>(a, m, lane, b, xs, xe, ring);
         else march::march_ring<NO, false, false>(a, m, lane, b, xs, xe, ring);
     }
+}
+
+template <int NO>
+__global__ void __launch_bounds__(128) fdfk_march_kernel(StepArgs a, MarchArgs m)
+{
+    march_warp<NO>(a, m, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
+}
+
+// The fast path over every member of a batch: member s owns blocks march_off[s] .. march_off[s+1]-1.
+template <int NO>
+__global__ void __launch_bounds__(128) fdfk_march_batch_kernel(BatchTab t)
+{
+    const int s = batch_member(t.march_off, t.n, blockIdx.x);
+    if (!t.live[s]) return;
+    march_warp<NO>(t.args[s], t.march[s], (blockIdx.x - t.march_off[s]) * (blockDim.x >> 5) + (threadIdx.x >> 5));
 }
 
 template <int NO>
@@ -199,6 +214,33 @@ int march_warp_slots(int norder)
     case 3: return warp_slots_no<3>();
     case 4: return warp_slots_no<4>();
     default: return 0;
+    }
+}
+
+template <int NO>
+static cudaError_t launch_march_batch_no(const BatchTab& t, int blocks, cudaStream_t s)
+{
+    const size_t smem = march_smem_bytes<NO>();
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(fdfk_march_batch_kernel<NO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    if (blocks == 0) return cudaSuccess;
+    fdfk_march_batch_kernel<NO><<<blocks, 128, smem, s>>>(t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_march_batch(const BatchTab& t, int norder, int blocks, cudaStream_t s)
+{
+    switch (norder) {
+    case 1: return launch_march_batch_no<1>(t, blocks, s);
+    case 2: return launch_march_batch_no<2>(t, blocks, s);
+    case 3: return launch_march_batch_no<3>(t, blocks, s);
+    case 4: return launch_march_batch_no<4>(t, blocks, s);
+    default: return cudaErrorInvalidValue;
     }
 }
 

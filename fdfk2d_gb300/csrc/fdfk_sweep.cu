@@ -195,16 +195,18 @@ __device__ void sample_receivers(const StepArgs& a, int blk)
 // ---------------------------------------------------------------------------
 // The step kernel.
 // ---------------------------------------------------------------------------
+// Block `blk` of one solve's tiled launch: a tile of the top band, an absorbing layer, or (past
+// n_tiles) a block of receivers.
 template <int NO>
-__global__ void __launch_bounds__(kThreads, 3) fdfk_step_kernel(StepArgs a)
+__device__ __forceinline__ void step_block(const StepArgs& a, int blk)
 {
     constexpr int H = 2 * NO - 1;
     extern __shared__ float sm[];
-    if ((int)blockIdx.x >= a.n_tiles) {
-        sample_receivers(a, blockIdx.x - a.n_tiles);
+    if (blk >= a.n_tiles) {
+        sample_receivers(a, blk - a.n_tiles);
         return;
     }
-    const Rect R = decode_tile(a, blockIdx.x);
+    const Rect R = decode_tile(a, blk);
     const TileDims T = tile_dims(NO, a.tdz[R.cls], a.tdx[R.cls]);
     const int TZ = T.TZ, TX = T.TX;
     const bool pml = R.side != 0;
@@ -594,6 +596,60 @@ __global__ void __launch_bounds__(kThreads, 3) fdfk_step_kernel(StepArgs a)
 #undef VZI
 }
 
+template <int NO>
+__global__ void __launch_bounds__(kThreads, 3) fdfk_step_kernel(StepArgs a)
+{
+    step_block<NO>(a, blockIdx.x);
+}
+
+// Largest s with off[s] <= blk (off[0] = 0, off[n] = total blocks).
+__device__ __forceinline__ int batch_member(const int* __restrict__ off, int n, int blk)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The tiled kernel over every member of a batch: member s owns blocks edge_off[s] .. edge_off[s+1]-1.
+template <int NO>
+__global__ void __launch_bounds__(kThreads, 3) fdfk_step_batch_kernel(BatchTab t)
+{
+    const int s = batch_member(t.edge_off, t.n, blockIdx.x);
+    if (!t.live[s]) return;
+    step_block<NO>(t.args[s], blockIdx.x - t.edge_off[s]);
+}
+
+// Per-step bookkeeping of a batch on the device: time index, plane parity and receiver sampling of
+// every member, written into its StepArgs before the step's kernels run.
+__global__ void fdfk_batch_bump(BatchTab t)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= t.n) return;
+    BatchDyn& d = t.dyn[s];
+    StepArgs& a = t.args[s];
+    if (!d.live || d.it > d.nt) {
+        d.live = 0;
+        t.live[s] = 0;
+        return;
+    }
+    a.it = d.it;
+    a.cur = d.cur;
+    a.nrcv = 0;
+    if (d.nrcv > 0 && d.isis == d.it && d.istp <= d.nsis) {
+        a.nrcv = d.nrcv;
+        a.sample_index = d.istp;
+        d.istp += 1;
+        d.isis += d.nstp;
+    }
+    t.live[s] = 1;
+    d.it += 1;
+    d.cur ^= 1;
+}
+
 // ---------------------------------------------------------------------------
 // Host-side launch helpers
 // ---------------------------------------------------------------------------
@@ -628,6 +684,50 @@ cudaError_t launch_step(const StepArgs& a, cudaStream_t s)
     case 8: return launch_no<8>(a, nsb, s);
     default: return cudaErrorInvalidValue;
     }
+}
+
+template <int NO>
+static cudaError_t launch_batch_no(const BatchTab& t, int blocks, size_t smem, cudaStream_t s)
+{
+    static int configured = 0;
+    if ((int)smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(fdfk_step_batch_kernel<NO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = (int)smem;
+    }
+    if (blocks == 0) return cudaSuccess;
+    fdfk_step_batch_kernel<NO><<<blocks, kThreads, smem, s>>>(t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step_batch(const BatchTab& t, int norder, int blocks, size_t smem, cudaStream_t s)
+{
+    switch (norder) {
+    case 1: return launch_batch_no<1>(t, blocks, smem, s);
+    case 2: return launch_batch_no<2>(t, blocks, smem, s);
+    case 3: return launch_batch_no<3>(t, blocks, smem, s);
+    case 4: return launch_batch_no<4>(t, blocks, smem, s);
+    case 5: return launch_batch_no<5>(t, blocks, smem, s);
+    case 6: return launch_batch_no<6>(t, blocks, smem, s);
+    case 7: return launch_batch_no<7>(t, blocks, smem, s);
+    case 8: return launch_batch_no<8>(t, blocks, smem, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_batch_bump(const BatchTab& t, cudaStream_t s)
+{
+    fdfk_batch_bump<<<(t.n + 127) / 128, 128, 0, s>>>(t);
+    return cudaGetLastError();
+}
+
+size_t step_smem_for(const StepArgs& a)
+{
+    size_t smem = 0;
+    for (int c = 0; c < 3; ++c)
+        smem = std::max(smem, sizeof(float) * (size_t)tile_dims(a.norder, a.tdz[c], a.tdx[c]).total);
+    return smem;
 }
 
 // Tile shapes and counts of the tiled kernel.  band_top: the fast path covers rows below

@@ -84,6 +84,31 @@ struct MarchArgs {
 // Tile shapes and counts of fdfk_step_kernel for a (fdfk_sweep.cu); needs nx, nz, npml, NX, int_rows.
 void plan_tiles(StepArgs& a, bool band_top);
 
+// Dynamic shared memory of a's tiled launch.
+size_t step_smem_for(const StepArgs& a);
+
+// Device-side per-member state of a batch (advanced by fdfk_batch_bump before every step).
+struct BatchDyn {
+    int live;                 // 0 once the member passed its last time index
+    int it, nt, cur;
+    int nrcv, nstp, nsis, isis, istp;
+};
+
+// Device tables of a batch (passed by value to the batched kernels).
+struct BatchTab {
+    int n;                    // members
+    StepArgs* args;           // [n] per-member arguments (time fields written by the bump kernel)
+    const MarchArgs* march;   // [n]
+    BatchDyn* dyn;            // [n]
+    int* live;                // [n] member takes part in the current step
+    const int* edge_off;      // [n+1] first tiled-kernel block of each member
+    const int* march_off;     // [n+1] first fast-path block of each member
+};
+
+cudaError_t launch_step_batch(const BatchTab& t, int norder, int blocks, size_t smem, cudaStream_t s);
+cudaError_t launch_batch_bump(const BatchTab& t, cudaStream_t s);
+cudaError_t launch_march_batch(const BatchTab& t, int norder, int blocks, cudaStream_t s);
+
 constexpr int kMarchSeg = 64;
 constexpr int kMarchMaxOrder = 4;
 

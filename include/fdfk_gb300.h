@@ -131,6 +131,38 @@ int fdfk_session_download_state(fdfk_session* s, float* ux, float* uz, float* co
 void fdfk_session_destroy(fdfk_session* s);
 
 /*
+ * Batches: many solves advanced together (events of one model, or models of
+ * different sizes), each solve the time loop of simulate_wavefield
+ * (src/FDFK2D.f90:465-532) on its own session.  No counterpart in the
+ * reference, which runs one solve per process.
+ *
+ * All members share `norder`.  A step of the batch is three kernel launches
+ * whatever the number of members (a bookkeeping kernel, the fast path and the
+ * tiled kernel over every member's cells); chunks of `graph chunk` steps are
+ * captured into a CUDA graph and replayed while the membership is unchanged.
+ * A member stops at its own last time index nt.  While a session is a member,
+ * calls that change it (advance, upload_*, set_receivers, fk_background) are
+ * refused with FDFK_ESTATE; downloads and fdfk_session_synchronize first wait
+ * for the batch.  Sessions must have their background for every remaining
+ * time index when added.
+ */
+typedef struct fdfk_batch fdfk_batch;
+int fdfk_batch_create(int norder, fdfk_batch** out);
+int fdfk_batch_add(fdfk_batch* b, fdfk_session* s);
+int fdfk_batch_remove(fdfk_batch* b, fdfk_session* s);
+/* Steps per captured graph (default 32; 0 launches step by step). */
+int fdfk_batch_set_graph_chunk(fdfk_batch* b, int steps);
+/* Advance every member by nsteps (a member past its nt does nothing). Asynchronous. */
+int fdfk_batch_advance(fdfk_batch* b, int nsteps);
+/* Wait for the batch and bring the members' step counters up to date. */
+int fdfk_batch_synchronize(fdfk_batch* b);
+/* Members that have not yet passed their last time index (synchronizes). */
+int fdfk_batch_live(fdfk_batch* b);
+int fdfk_batch_size(const fdfk_batch* b);
+/* Releases the batch; its members become ordinary sessions again. */
+void fdfk_batch_destroy(fdfk_batch* b);
+
+/*
  * The whole time loop of simulate_wavefield (src/FDFK2D.f90:465-532) in one
  * call: host material and background in, host seismograms out, state zeroed
  * at the start as in src/FDFK2D.f90:280-300.  seisx/seisz are (nsis+1) x nrcv.
