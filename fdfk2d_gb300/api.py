@@ -61,6 +61,23 @@ class FkParams(C.Structure):
                    float(p["rayp"]))
 
 
+class SolveRequest(C.Structure):
+    """fdfk_solve_request: one solve for the serving loop."""
+    _fields_ = [("p", Params), ("c", C.c_void_p), ("fk", FkParams), ("bazs", C.c_void_p),
+                ("nlayer_left", C.c_int), ("fk_left", C.c_void_p), ("nlayer_right", C.c_int),
+                ("fk_right", C.c_void_p), ("nrcv", C.c_int), ("rx", C.c_void_p), ("rz", C.c_void_p),
+                ("x0", C.c_float), ("z0", C.c_float), ("nstp", C.c_int), ("nsis", C.c_int),
+                ("seisx", C.c_void_p), ("seisz", C.c_void_p)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("queued", C.c_int), ("running", C.c_int), ("completed", C.c_longlong), ("failed", C.c_longlong),
+                ("bytes_in_use", C.c_longlong), ("budget", C.c_longlong)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
 def _fk_model(m, name):
     m = np.asfortranarray(m, np.float32)
     if m.ndim != 2 or m.shape[0] != 4:
@@ -87,6 +104,8 @@ def lib():
         L.fdfk_kernel_launches.restype = C.c_longlong
         L.fdfk_session_create.argtypes = [C.POINTER(Params), C.c_void_p, C.POINTER(C.c_void_p)]
         L.fdfk_batch_destroy.restype = None
+        L.fdfk_server_destroy.restype = None
+        L.fdfk_session_device_bytes.restype = C.c_longlong
         for name in ("fdfk_session_set_stream", "fdfk_session_advance", "fdfk_session_synchronize",
                      "fdfk_session_step_index", "fdfk_session_destroy", "fdfk_session_upload_background",
                      "fdfk_session_set_receivers", "fdfk_session_download_seismograms",
@@ -94,7 +113,9 @@ def lib():
                      "fdfk_session_download_seismogram_range", "fdfk_session_advance_timed",
                      "fdfk_session_interior_cells", "fdfk_session_fk_background", "fdfk_fk_background",
                      "fdfk_batch_create", "fdfk_batch_add", "fdfk_batch_remove", "fdfk_batch_set_graph_chunk",
-                     "fdfk_batch_advance", "fdfk_batch_synchronize", "fdfk_batch_live", "fdfk_batch_size"):
+                     "fdfk_batch_advance", "fdfk_batch_synchronize", "fdfk_batch_live", "fdfk_batch_size",
+                     "fdfk_server_create", "fdfk_server_submit", "fdfk_server_pump", "fdfk_server_request",
+                     "fdfk_server_get_stats"):
             getattr(L, name).restype = C.c_int if name != "fdfk_session_destroy" else None
         _lib = L
     return _lib
@@ -279,6 +300,96 @@ class Batch:
             lib().fdfk_batch_destroy(self._h)
             self._h = None
             self.members = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def session_device_bytes(p: dict, nrcv: int, nsis: int) -> int:
+    """Device bytes a session of these parameters holds (what the server's budget counts)."""
+    prm = Params.from_dict(p)
+    return int(lib().fdfk_session_device_bytes(C.byref(prm), C.c_int(nrcv), C.c_int(nsis)))
+
+
+class Server:
+    """Serving loop (fdfk_server): requests are admitted by device-memory budget into one running
+    batch, advanced `chunk` steps per pump, and retired into host seismogram arrays when done."""
+
+    def __init__(self, norder: int, budget_bytes: int, chunk: int = 32):
+        h = C.c_void_p()
+        _check(lib().fdfk_server_create(C.c_int(int(norder)), C.c_longlong(int(budget_bytes)), C.c_int(int(chunk)),
+                                        C.byref(h)))
+        self._h = h
+        self._req = {}
+
+    def submit(self, p: dict, c, fk: dict, bazs, fk_left, fk_right, rx, rz, x0: float = 0.0, z0: float = 0.0,
+               nstp: int = 1, nsis: int | None = None) -> int:
+        """Queue one solve; returns its id.  The arrays are kept alive until the request finishes."""
+        if nsis is None:
+            nsis = int(p["nt"]) // nstp
+        keep = {"c": np.asfortranarray(c, np.float32), "bazs": np.ascontiguousarray(bazs, np.float64),
+                "fl": _fk_model(fk_left, "fk_left"), "fr": _fk_model(fk_right, "fk_right"),
+                "rx": np.ascontiguousarray(rx, np.float32), "rz": np.ascontiguousarray(rz, np.float32)}
+        nrcv = keep["rx"].size
+        keep["sx"] = np.zeros((nsis + 1, nrcv), np.float32, order="F")
+        keep["sz"] = np.zeros((nsis + 1, nrcv), np.float32, order="F")
+        r = SolveRequest()
+        r.p = Params.from_dict(p)
+        r.c = keep["c"].ctypes.data
+        r.fk = FkParams.from_dict(fk)
+        r.bazs = keep["bazs"].ctypes.data
+        r.nlayer_left, r.fk_left = keep["fl"].shape[1], keep["fl"].ctypes.data
+        r.nlayer_right, r.fk_right = keep["fr"].shape[1], keep["fr"].ctypes.data
+        r.nrcv, r.rx, r.rz = nrcv, keep["rx"].ctypes.data, keep["rz"].ctypes.data
+        r.x0, r.z0, r.nstp, r.nsis = float(x0), float(z0), int(nstp), int(nsis)
+        r.seisx, r.seisz = keep["sx"].ctypes.data, keep["sz"].ctypes.data
+        rid = C.c_longlong()
+        _check(lib().fdfk_server_submit(self._h, C.byref(r), C.byref(rid)))
+        self._req[rid.value] = keep
+        return rid.value
+
+    def pump(self) -> int:
+        n = C.c_int()
+        _check(lib().fdfk_server_pump(self._h, C.byref(n)))
+        return n.value
+
+    def request(self, rid: int):
+        """(state, t_submit, t_admit, t_done) on the host steady clock (seconds)."""
+        st = C.c_int()
+        t = [C.c_double() for _ in range(3)]
+        _check(lib().fdfk_server_request(self._h, C.c_longlong(rid), C.byref(st), *[C.byref(x) for x in t]))
+        return st.value, t[0].value, t[1].value, t[2].value
+
+    def result(self, rid: int):
+        """Seismograms (seisx, seisz) of a finished request."""
+        state = self.request(rid)[0]
+        if state != REQ_DONE:
+            raise FDFKError(-5 if state != REQ_FAILED else -1, f"request {rid} is not done (state {state})")
+        keep = self._req[rid]
+        return keep["sx"], keep["sz"]
+
+    def release(self, rid: int):
+        """Drop the host arrays of a finished request."""
+        self._req.pop(rid, None)
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().fdfk_server_get_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fdfk_server_destroy(self._h)
+            self._h = None
 
     def __del__(self):
         try:

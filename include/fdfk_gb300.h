@@ -205,6 +205,61 @@ int fdfk_session_fk_background(fdfk_session* s, const fdfk_fk_params* p, const d
                                const float* fk_left, int nlayer_right, const float* fk_right);
 
 /*
+ * Serving: solve requests (a model, an incident plane wave, receivers) are
+ * queued, admitted in arrival order while their device memory fits the
+ * budget (fdfk_session_device_bytes: material, wavefield, absorbing-layer
+ * state, the FK background of every time step, seismograms), joined to one
+ * running batch and retired into the caller's buffers when done.  No
+ * counterpart in the reference.  Each fdfk_server_pump call retires finished
+ * solves (waiting for the chunk launched by the previous pump), admits what
+ * fits, and launches the next chunk of steps asynchronously; requests that
+ * arrive between pumps join the running batch at the next pump.  Every
+ * pointer of a request must stay valid until its state is DONE or FAILED.
+ * The FK background of an admitted request is computed on the GPU.
+ */
+#define FDFK_REQ_QUEUED 0
+#define FDFK_REQ_RUNNING 1
+#define FDFK_REQ_DONE 2
+#define FDFK_REQ_FAILED 3
+
+typedef struct fdfk_solve_request {
+    fdfk_params p;                 /* grid, stencil, PML; nt = last time index */
+    const float* c;                /* c(1:3, NZ, NX) = rho, lambda, mu */
+    fdfk_fk_params fk;             /* FK background (geometry as p) */
+    const double* bazs;            /* nx + 2 npml back-azimuths (rad) */
+    int nlayer_left;
+    const float* fk_left;          /* (4, nlayer_left) */
+    int nlayer_right;
+    const float* fk_right;         /* (4, nlayer_right) */
+    int nrcv;                      /* receivers, as fdfk_session_set_receivers */
+    const float* rx;
+    const float* rz;
+    float x0, z0;
+    int nstp, nsis;
+    float* seisx;                  /* outputs (nsis+1) x nrcv, written when the solve is done */
+    float* seisz;
+} fdfk_solve_request;
+
+typedef struct fdfk_server_stats {
+    int queued, running;
+    long long completed, failed;
+    long long bytes_in_use, budget;
+} fdfk_server_stats;
+
+typedef struct fdfk_server fdfk_server;
+
+/* Device bytes one session of these parameters holds (nrcv receivers, nsis+1 samples). */
+long long fdfk_session_device_bytes(const fdfk_params* p, int nrcv, int nsis);
+int fdfk_server_create(int norder, long long hbm_budget_bytes, int chunk_steps, fdfk_server** out);
+int fdfk_server_submit(fdfk_server* s, const fdfk_solve_request* r, long long* id);
+/* Retire, admit, launch one chunk; *in_flight = queued + running requests afterwards. */
+int fdfk_server_pump(fdfk_server* s, int* in_flight);
+/* State (FDFK_REQ_*) and host steady-clock times (s) of submission, admission and completion. */
+int fdfk_server_request(fdfk_server* s, long long id, int* state, double* t_submit, double* t_admit, double* t_done);
+int fdfk_server_get_stats(const fdfk_server* s, fdfk_server_stats* st);
+void fdfk_server_destroy(fdfk_server* s);
+
+/*
  * Drop-in for lib_gnu/libFK3D.so's comput_background_wavefield_ (32
  * arguments, gfortran ABI, by reference; call at src/FDFK2D.f90:429-431).
  * Prints a message and aborts on failure, as a Fortran `stop` would.
