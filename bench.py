@@ -133,6 +133,109 @@ def cpu_reference(w, budget_s=15.0, max_steps=40):
                          f"({dt:.1f} s, OMP threads={cores})"
 
 
+def batched_and_served(F, WL, args, torch, dev):
+    """Config 3 (64 events on the config-1 model, batched vs sequential plain-GPU solves, each
+    solve from host inputs to host seismograms including its FK background on the GPU) and
+    config 5 (an open-loop Poisson stream of config-3 requests through the serving loop at 80 %
+    of the measured batched capacity, 160 GB admission budget)."""
+    w1 = WL.config1()
+    p1 = w1["p"]
+    nt = p1["nt"]
+    cells1 = (p1["nz"] + p1["npml"]) * (p1["nx"] + 2 * p1["npml"])
+    events = WL.config3_events(args.batch_events)
+    rx, rz = w1["rx"], w1["rz"]
+    out = {}
+
+    def solve_inputs(ev):
+        fp, bazs, fl, fr = WL.event_inputs(w1, ev)
+        return fp, bazs, fl, fr
+
+    # sequential plain-GPU solves (a bounded sample, same events)
+    nseq = min(args.seq_sample, len(events))
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for ev in events[:nseq]:
+        fp, bazs, fl, fr = solve_inputs(ev)
+        with F.Session(p1, w1["c"]) as s:
+            s.fk_background(fp, bazs, fl, fr)
+            s.set_receivers(rx, rz, w1["x0"], w1["z0"], 1, nt)
+            s.advance(nt + 1)
+            s.seismograms()
+    t_seq = (time.perf_counter() - t0) / nseq
+    # batched: every event at once
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    sessions = []
+    b = F.Batch(p1["norder"])
+    for ev in events:
+        fp, bazs, fl, fr = solve_inputs(ev)
+        s = F.Session(p1, w1["c"])
+        s.fk_background(fp, bazs, fl, fr)
+        s.set_receivers(rx, rz, w1["x0"], w1["z0"], 1, nt)
+        b.add(s)
+        sessions.append(s)
+    b.advance(nt + 1)
+    traces = [s.seismograms() for s in sessions]
+    t_batch = time.perf_counter() - t0
+    b.close()
+    for s in sessions:
+        s.close()
+    assert all(np.isfinite(tz).all() for _, tz in traces)
+    n = len(events)
+    out["batched"] = {"workload": f"config3: {n} events (P 0.04-0.08, S 0.10-0.12 s/km, baz 0-360, 0.5-1 Hz) "
+                                  f"on the config-1 model, nt={nt}",
+                      "solves_per_hour": round(n / t_batch * 3600, 1), "wall_s": round(t_batch, 3),
+                      "mcell_steps_per_s": round(n * cells1 * (nt + 1) / t_batch / 1e6, 1),
+                      "sequential_solves_per_hour": round(3600 / t_seq, 1), "sequential_sample": nseq,
+                      "speedup_vs_sequential": round(t_seq * n / t_batch, 2),
+                      "note": "each solve from host inputs to host seismograms, FK background on the GPU"}
+    if args.serve_requests <= 0:
+        return out
+    # serving: open-loop Poisson arrivals at 80 % of the batched capacity
+    cap = n / t_batch
+    rate = 0.8 * cap
+    rng = np.random.default_rng(11)
+    reqs = WL.config3_events(args.serve_requests, seed=13)
+    rng.shuffle(reqs)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+    srv = F.Server(p1["norder"], budget_bytes=160 << 30, chunk=64)
+    ids, sched, peak = [], [], 0
+    t0 = time.monotonic()
+    i = 0
+    while True:
+        now = time.monotonic() - t0
+        while i < len(reqs) and arrivals[i] <= now:
+            fp, bazs, fl, fr = solve_inputs(reqs[i])
+            ids.append(srv.submit(p1, w1["c"], fp, bazs, fl, fr, rx, rz, w1["x0"], w1["z0"], 1, nt))
+            sched.append(t0 + arrivals[i])
+            i += 1
+        left = srv.pump()
+        peak = max(peak, srv.stats()["running"])
+        if left == 0:
+            if i >= len(reqs):
+                break
+            time.sleep(max(0.0, min(0.05, arrivals[i] - (time.monotonic() - t0))))
+    t_all = time.monotonic() - t0
+    lat = []
+    for rid, ta in zip(ids, sched):
+        st, _, _, t_done = srv.request(rid)
+        assert st == F.api.REQ_DONE
+        lat.append(t_done - ta)
+        srv.release(rid)
+    srv.close()
+    lat = np.array(lat)
+    out["serving"] = {"workload": f"config5 (scaled): {len(reqs)} Poisson requests drawn from config 3, "
+                                  f"arrival rate {rate:.2f}/s = 80 % of the batched capacity, budget 160 GB",
+                      "requests": len(reqs), "arrival_rate_per_s": round(rate, 3),
+                      "solves_per_hour": round(len(reqs) / t_all * 3600, 1),
+                      "p50_s": round(float(np.percentile(lat, 50)), 3),
+                      "p95_s": round(float(np.percentile(lat, 95)), 3),
+                      "p99_s": round(float(np.percentile(lat, 99)), 3),
+                      "max_running": peak, "wall_s": round(t_all, 2),
+                      "sequential_solves_per_hour": out["batched"]["sequential_solves_per_hour"]}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -142,6 +245,9 @@ def main():
     ap.add_argument("--workload", default="config2", choices=["config2", "config1"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fk-full", action="store_true")
+    ap.add_argument("--batch-events", type=int, default=64, help="config-3 events (0: skip batched and serving)")
+    ap.add_argument("--seq-sample", type=int, default=8, help="sequential solves timed for the comparison")
+    ap.add_argument("--serve-requests", type=int, default=192, help="config-5 requests (0: skip serving)")
     args = ap.parse_args()
     K, Wm = args.steps, max(3, args.warmup)
 
@@ -264,6 +370,10 @@ def main():
             n_fft *= 2
         series = sum(int(np.prod(s_[:2])) for s_ in F.strip_shapes(p["nx"], p["nz"], p["nbd"], p["nt"]).values())
 
+    extra = None
+    if rank == 0 and args.batch_events > 0:
+        extra = batched_and_served(F, WL, args, torch, dev)
+
     peak, peak_kind = measured_peak()
     # dominant kernel: the interior fast path (its own cells, its own event-timed duration)
     if cells_int > 0 and ms_int > 0:
@@ -292,6 +402,8 @@ def main():
                              "whole_step_equiv_gbs": round(step_equiv, 1),
                              "whole_step_frac": round(step_equiv / peak, 4)},
                 "cpu_baseline": cpu, "clocks": clk}
+        if extra:
+            line.update(extra)
         if fk_ms is not None:
             line["fk_background"] = {"ms": round(fk_ms, 1), "nt": p["nt"], "series": series, "n_fft": n_fft,
                                      "precision": "fp64 spectra and transforms, f32 strips",

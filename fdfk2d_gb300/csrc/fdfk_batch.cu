@@ -18,6 +18,10 @@
 
 using namespace fdfk;
 
+namespace fdfk {
+int march_warp_slots(int norder);
+}
+
 struct fdfk_batch {
     int norder = 0;
     std::vector<fdfk_session*> members;
@@ -122,6 +126,16 @@ int rebuild(fdfk_batch* b)
     std::vector<BatchDyn> dyn(n);
     std::vector<int> live(n, 0), eoff(n + 1, 0), moff(n + 1, 0);
     size_t smem = 0;
+    // fast-path segments re-planned for the whole batch: about two waves of resident warps over
+    // all members' work, 16..48 columns per segment (a member alone plans for itself only)
+    long long work = 0;
+    for (const fdfk_session* s : b->members) work += (long long)s->p.nx * s->march.n_bands;
+    const int slots = b->norder <= kMarchMaxOrder ? march_warp_slots(b->norder) : 0;
+    int seg = kMarchSeg;
+    if (slots > 0) {
+        seg = (int)((work + 2LL * slots - 1) / (2LL * slots));
+        seg = seg < 16 ? 16 : seg > 48 ? 48 : seg;
+    }
     for (int i = 0; i < n; ++i) {
         const fdfk_session* s = b->members[i];
         StepArgs a = s->base;
@@ -136,7 +150,12 @@ int rebuild(fdfk_batch* b)
         a.rx = s->rx; a.rz = s->rz;
         a.seisx = s->seisx; a.seisz = s->seisz;
         args[i] = a;
-        march[i] = s->march;
+        MarchArgs m = s->march;
+        if (m.n_bands > 0) {
+            m.seg_len = seg;
+            m.n_segs = (s->p.nx + seg - 1) / seg;
+        }
+        march[i] = m;
         BatchDyn d{};
         d.it = s->it; d.nt = s->p.nt; d.cur = s->cur;
         d.nrcv = s->nrcv; d.nstp = s->nstp; d.nsis = s->nsis; d.isis = s->isis; d.istp = s->istp;
@@ -144,7 +163,7 @@ int rebuild(fdfk_batch* b)
         dyn[i] = d;
         const int nsb = s->nrcv > 0 ? (s->nrcv + kThreads - 1) / kThreads : 0;
         eoff[i + 1] = eoff[i] + a.n_tiles + nsb;
-        moff[i + 1] = moff[i] + (s->march.n_bands * s->march.n_segs + 3) / 4;
+        moff[i + 1] = moff[i] + (m.n_bands * m.n_segs + 3) / 4;
         smem = std::max(smem, step_smem_for(a));
     }
     if (n) {
@@ -221,7 +240,13 @@ int fdfk_batch_add(fdfk_batch* b, fdfk_session* s)
         if (!s->have_bg[t]) return set_error(FDFK_ESTATE, "the session has no background for time index " + std::to_string(t));
     int rc = pull(b);
     if (rc) return rc;
-    BK(cudaStreamSynchronize(s->stream));   // the session's own uploads have landed
+    // the batch's next step waits for the session's own uploads and FK background (no host wait)
+    cudaEvent_t ready = nullptr;
+    BK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ready, s->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, ready, 0);
+    cudaEventDestroy(ready);
+    if (e != cudaSuccess) return set_error(FDFK_ECUDA, std::string("batch add: ") + cudaGetErrorString(e));
     b->members.push_back(s);
     s->batch = b;
     b->dirty = true;

@@ -178,8 +178,8 @@ void damping(const fdfk_params& p, std::vector<DampCol>& dx, std::vector<DampCol
     const double Lx = (double)p.npml * p.dx, Lz = (double)p.npml * p.dz;
     const double d0x = (p.npower + 1) * (double)p.vpml * lg / (2.0 * Lx);
     const double d0z = (p.npower + 1) * (double)p.vpml * lg / (2.0 * Lz);
-    dx.assign(NX, DampCol{0.f, 0.f});
-    dz.assign(NZ, DampCol{0.f, 0.f});
+    dx.assign(NX, make_damp(0.f, 0.f));
+    dz.assign(NZ, make_damp(0.f, 0.f));
     for (int c = 0; c < NX; ++c) {
         int ix = c + 1 - p.npml;
         double s = 0.0, sg = 0.0;
@@ -187,14 +187,14 @@ void damping(const fdfk_params& p, std::vector<DampCol>& dx, std::vector<DampCol
         else if (ix > p.nx) { s = (double)(ix - p.nx) * p.dx / Lx; sg = 1.0; }
         else continue;
         double d = d0x * std::pow(s, p.npower), dp = p.npower * d0x * std::pow(s, p.npower - 1) / Lx;
-        dx[c] = DampCol{(float)(d * p.dt), (float)(sg * dp * p.dt)};
+        dx[c] = make_damp((float)(d * p.dt), (float)(sg * dp * p.dt));
     }
     for (int r = 0; r < NZ; ++r) {
         int iz = r + 1;
         if (iz <= p.nz) continue;
         double s = (double)(iz - p.nz) * p.dz / Lz;
         double d = d0z * std::pow(s, p.npower), dp = p.npower * d0z * std::pow(s, p.npower - 1) / Lz;
-        dz[r] = DampCol{(float)(d * p.dt), (float)(dp * p.dt)};
+        dz[r] = make_damp((float)(d * p.dt), (float)(dp * p.dt));
     }
 }
 

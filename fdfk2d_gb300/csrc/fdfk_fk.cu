@@ -27,6 +27,9 @@
 #include <cmath>
 #include <complex>
 #include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 namespace fdfk {
@@ -446,25 +449,62 @@ int build_layers(const float* model, int L, double rayp, std::vector<FkLayer>& o
     return FDFK_OK;
 }
 
+// Work buffers of one call, stream-ordered: allocated and released on the call's stream, so the
+// call neither waits for nor blocks other streams.
 struct DevBufs {
+    cudaStream_t stream = nullptr;
     std::vector<void*> ptrs;
-    cufftHandle plans[2] = {0, 0};
-    bool have_plan[2] = {false, false};
+    explicit DevBufs(cudaStream_t s) : stream(s) {}
     ~DevBufs()
     {
-        for (int i = 0; i < 2; ++i)
-            if (have_plan[i]) cufftDestroy(plans[i]);
-        for (void* p : ptrs) cudaFree(p);
+        for (void* p : ptrs) cudaFreeAsync(p, stream);
     }
     template <class T>
     cudaError_t alloc(T** p, size_t n)
     {
         *p = nullptr;
-        cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
+        cudaError_t e = cudaMallocAsync((void**)p, std::max<size_t>(n, 1) * sizeof(T), stream);
         if (e == cudaSuccess) ptrs.push_back(*p);
         return e;
     }
 };
+
+// Batched Z2D plans, one per (device, length, batch), kept for the life of the process.  They
+// own no work area: each call supplies its own (stream-ordered), so calls on different streams
+// may use one plan at the same time.
+struct Z2DPlan {
+    cufftHandle h = 0;
+    size_t work = 0;
+};
+
+std::mutex g_plan_mu;
+std::map<std::tuple<int, int, int>, Z2DPlan> g_plans;
+
+cufftResult z2d_plan(int n, int batch, Z2DPlan& out)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(g_plan_mu);
+    const auto key = std::make_tuple(dev, n, batch);
+    auto it = g_plans.find(key);
+    if (it != g_plans.end()) {
+        out = it->second;
+        return CUFFT_SUCCESS;
+    }
+    Z2DPlan p;
+    cufftResult r = cufftCreate(&p.h);
+    if (r != CUFFT_SUCCESS) return r;
+    int nn = n, inembed = n / 2 + 1, onembed = n;
+    if ((r = cufftSetAutoAllocation(p.h, 0)) != CUFFT_SUCCESS ||
+        (r = cufftMakePlanMany(p.h, 1, &nn, &inembed, 1, n / 2 + 1, &onembed, 1, n, CUFFT_Z2D, batch, &p.work)) !=
+            CUFFT_SUCCESS) {
+        cufftDestroy(p.h);
+        return r;
+    }
+    g_plans[key] = p;
+    out = p;
+    return CUFFT_SUCCESS;
+}
 
 }  // namespace
 
@@ -600,7 +640,7 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
     tab.bottom_pos = cbar >= 0.0 ? 1 : 0;
     const long long nseries = tab.off[NSTRIP];
 
-    DevBufs B;
+    DevBufs B(stream);
     FkLayer *d_lay0, *d_lay1;
     double *d_w, *d_esc, *d_cos, *d_D, *d_y;
     cd *d_tw, *d_W, *d_amp0, *d_amp1, *d_U, *d_Ph, *d_spec;
@@ -653,27 +693,25 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
     const int nb_full = (int)std::min<long long>(bmax, 65535);
     FK_CK(B.alloc(&d_spec, (size_t)nb_full * (g.nh + 1)));
     FK_CK(B.alloc(&d_y, (size_t)nb_full * g.N));
-    int n_fft = g.N, inembed = g.nh + 1, onembed = g.N;
-    FFT_CK(cufftPlanMany(&B.plans[0], 1, &n_fft, &inembed, 1, g.nh + 1, &onembed, 1, g.N, CUFFT_Z2D, nb_full));
-    B.have_plan[0] = true;
-    FFT_CK(cufftSetStream(B.plans[0], stream));
     const int tail = (int)(nseries % nb_full);
-    if (tail && nseries > nb_full) {
-        FFT_CK(cufftPlanMany(&B.plans[1], 1, &n_fft, &inembed, 1, g.nh + 1, &onembed, 1, g.N, CUFFT_Z2D, tail));
-        B.have_plan[1] = true;
-        FFT_CK(cufftSetStream(B.plans[1], stream));
-    }
+    Z2DPlan plan_full, plan_tail;
+    FFT_CK(z2d_plan(g.N, nb_full, plan_full));
+    if (tail && nseries > nb_full) FFT_CK(z2d_plan(g.N, tail, plan_tail));
+    void* work = nullptr;
+    FK_CK(B.alloc(reinterpret_cast<char**>(&work), std::max(plan_full.work, plan_tail.work)));
     for (long long g0 = 0; g0 < nseries; g0 += nb_full) {
         const int nb = (int)std::min<long long>(nb_full, nseries - g0);
         const dim3 ga((g.nh + 1 + 255) / 256, nb);
         fk_assemble<<<ga, 256, 0, stream>>>(g, tab, g0, nb, d_U, d_Ph, d_cos, d_spec);
-        FFT_CK(cufftExecZ2D(nb == nb_full ? B.plans[0] : B.plans[1], (cufftDoubleComplex*)d_spec, d_y));
+        const Z2DPlan& pl = nb == nb_full ? plan_full : plan_tail;
+        FFT_CK(cufftSetWorkArea(pl.h, work));
+        FFT_CK(cufftSetStream(pl.h, stream));
+        FFT_CK(cufftExecZ2D(pl.h, (cufftDoubleComplex*)d_spec, d_y));
         const dim3 ge((J.nt + 1 + 31) / 32, (nb + 31) / 32);
         fk_epilogue<<<ge, dim3(32, 8), 0, stream>>>(tab, g0, nb, g.N, J.nt, d_y, d_esc);
         nl += 2;
         FK_CK(cudaGetLastError());
     }
-    FK_CK(cudaStreamSynchronize(stream));
     if (launches) *launches += nl;
     return FDFK_OK;
 }

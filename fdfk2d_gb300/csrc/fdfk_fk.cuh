@@ -37,8 +37,9 @@ struct FkJob {
 size_t fk_strip_elems(int nx, int nz, int nbd, int k);
 
 // Computes the 12 strips into device arrays dst[k] (reference layout, time slowest,
-// (nt + 1) samples) on `stream`.  Returns 0 or a negative FDFK_E* status with
-// `err` set.  `launches` is incremented by the number of kernels launched.
+// (nt + 1) samples), enqueued on `stream` (work buffers stream-ordered; the call
+// returns without waiting for the GPU).  Returns 0 or a negative FDFK_E* status
+// with `err` set.  `launches` is incremented by the number of kernels launched.
 int fk_background(const FkJob& job, float* const dst[12], cudaStream_t stream, std::string& err,
                   long long* launches);
 

@@ -154,7 +154,7 @@ size_t noalloc_floats_needed(const fdfk_params& p)
     size_t tot = up64(3 * n) + up64(4 * n);
     tot += 2 * (12 * up64(side) + 6 * up64(tb));                       // bu planes (l, r, b)
     tot += 4 * up64(side) + 4 * up64(tb);                              // bp (l, r, b)
-    tot += up64(2 * NX) + up64(2 * NZ);                                // damping
+    tot += up64(4 * NX) + up64(4 * NZ);                                // damping
     tot += 4 * up64((nz - nbd) * nbd) + 2 * up64(nbd * nx) + 4 * up64(nz * nbd) + 2 * up64(nbd * (nx + 2 * nbd));
     tot += up64(3 * NZ * NX) + 2 * up64(2 * NZ * NX);                  // raw c, ux, uz
     tot += 12 * up64(2 * side) + 6 * up64(2 * tb);                     // raw bu
@@ -206,8 +206,8 @@ int step_noalloc(const fdfk_params& p, int it, const float* const strips[12], co
     float* bpp[12] = {};
     for (int k = 0; k < 12; ++k)
         if (k < 4 || k >= 8) bpp[k] = take(k < 4 ? side : tb);
-    DampCol* dampx = reinterpret_cast<DampCol*>(take(2 * (size_t)NX));
-    DampCol* dampz = reinterpret_cast<DampCol*>(take(2 * (size_t)NZ));
+    DampCol* dampx = reinterpret_cast<DampCol*>(take(4 * (size_t)NX));
+    DampCol* dampz = reinterpret_cast<DampCol*>(take(4 * (size_t)NZ));
     float* sp[NSTRIP];
     size_t per[NSTRIP];
     for (int k = 0; k < NSTRIP; ++k) {
@@ -234,20 +234,20 @@ int step_noalloc(const fdfk_params& p, int it, const float* const strips[12], co
         for (int cx = 0; cx < NX; ++cx) {
             const int ix = cx + 1 - p.npml;
             double s = 0.0, sg = 0.0;
-            g_na_dampx[cx] = DampCol{0.f, 0.f};
+            g_na_dampx[cx] = make_damp(0.f, 0.f);
             if (ix <= 0) { s = (double)(1 - ix) * p.dx / Lx; sg = -1.0; }
             else if (ix > p.nx) { s = (double)(ix - p.nx) * p.dx / Lx; sg = 1.0; }
             else continue;
             const double d = d0x * std::pow(s, p.npower), dp = p.npower * d0x * std::pow(s, p.npower - 1) / Lx;
-            g_na_dampx[cx] = DampCol{(float)(d * p.dt), (float)(sg * dp * p.dt)};
+            g_na_dampx[cx] = make_damp((float)(d * p.dt), (float)(sg * dp * p.dt));
         }
         for (int r = 0; r < NZ; ++r) {
             const int iz = r + 1;
-            g_na_dampz[r] = DampCol{0.f, 0.f};
+            g_na_dampz[r] = make_damp(0.f, 0.f);
             if (iz <= p.nz) continue;
             const double s = (double)(iz - p.nz) * p.dz / Lz;
             const double d = d0z * std::pow(s, p.npower), dp = p.npower * d0z * std::pow(s, p.npower - 1) / Lz;
-            g_na_dampz[r] = DampCol{(float)(d * p.dt), (float)(dp * p.dt)};
+            g_na_dampz[r] = make_damp((float)(d * p.dt), (float)(dp * p.dt));
         }
     }
     NA_CK(cudaMemcpyAsync(dampx, g_na_dampx, NX * sizeof(DampCol), cudaMemcpyHostToDevice, st));

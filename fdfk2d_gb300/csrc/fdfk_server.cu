@@ -104,7 +104,7 @@ long long fdfk_session_device_bytes(const fdfk_params* p, int nrcv, int nsis)
     const long long strips = 4 * (nz - nbd) * nbd + 2 * nbd * nx + 4 * nz * nbd + 2 * nbd * (nx + 2 * nbd);
     long long f = 7 * n + 2 * (12 * side + 6 * tb) + 4 * side + 4 * tb + strips * (p->nt + 1LL);
     f += 2LL * nrcv + (nrcv > 0 ? 2LL * (nsis + 1) * nrcv : 0);
-    return 4 * f + 8 * (NX + NZ);
+    return 4 * f + (long long)sizeof(DampCol) * (NX + NZ);
 }
 
 int fdfk_server_create(int norder, long long hbm_budget_bytes, int chunk_steps, fdfk_server** out)

@@ -368,6 +368,9 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         const size_t g = gidx(a, iz, ix);
         const int nxo = ordx(a, ix, NO);
         const int nzo = ordz(a, iz, NO);
+        // every column ix-NO..ix (row iz-NO..iz) has the full order: no reduced-order half points
+        const bool fullx = ix - NO >= NO - npml + 1 && ix <= nx + npml - NO;
+        const bool fullz = iz - NO >= NO + 1 && iz <= NZ - NO;
 
         if (pml && (ix == 1 - npml || ix == nx + npml || iz == NZ)) {
             // outer frame: never advanced; keep level 1 across the plane swap
@@ -384,8 +387,8 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             float pa = GXI(gxA, z, x + k - 1), pb = GXI(gxB, z, x + k - 1);
             float ma, mb;
             int Lm = x - k;
-            int nr = ordx(a, ix - k + 1, NO);
-            if (nr == ordx(a, ix - k, NO)) {
+            int nr = fullx ? NO : ordx(a, ix - k + 1, NO);
+            if (fullx || nr == ordx(a, ix - k, NO)) {
                 ma = GXI(gxA, z, Lm); mb = GXI(gxB, z, Lm);
             } else {
                 float s1 = 0.f, s2 = 0.f;
@@ -411,8 +414,8 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             float pa = GZI(gzA, z + k - 1, x), pb = GZI(gzB, z + k - 1, x);
             float ma, mb;
             int Lm = z - k;
-            int nr = ordz(a, iz - k + 1, NO);
-            if (nr == ordz(a, iz - k, NO)) {
+            int nr = fullz ? NO : ordz(a, iz - k + 1, NO);
+            if (fullz || nr == ordz(a, iz - k, NO)) {
                 ma = GZI(gzA, Lm, x); mb = GZI(gzB, Lm, x);
             } else {
                 float s1 = 0.f, s2 = 0.f;
@@ -499,8 +502,9 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         // ---- PML cell: split-field update ----------------------------------
         const int side = R.side;
         const DampCol dxc = a.dampx[ix + npml - 1];
-        const DampCol dzc = side == 3 ? a.dampz[iz - 1] : DampCol{0.f, 0.f};
+        const DampCol dzc = side == 3 ? a.dampz[iz - 1] : DampCol{0.f, 0.f, 1.f, 1.f};
         const float yx = dxc.y, yz = dzc.y;
+        const float r2 = side == 3 ? fast_rcp(1.0f + 0.5f * (yx + yz)) : dxc.rh;   // 1 / (1 + (yx + yz)/2)
         size_t ap;
         if (side == 1) ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - (1 - npml));
         else if (side == 2) ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - nx - 1);
@@ -516,7 +520,7 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             dzux = fmaf(cz, SU(sux, z + k, x) - SU(sux, z - k, x), dzux);
             dzuz = fmaf(cz, SU(suz, z + k, x) - SU(suz, z - k, x), dzuz);
         }
-        dxux /= dx; dxuz /= dx; dzux /= dz; dzuz /= dz;
+        dxux *= rdx; dxuz *= rdx; dzux *= rdz; dzuz *= rdz;
         const float lam0 = SM(sLam, z, x), mu0 = SM(sMu, z, x), l2m0 = lam0 + 2.0f * mu0;
 
         const int base = side == 1 ? 0 : side == 2 ? 6 : 12;
@@ -553,7 +557,7 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             (void)lam0;
             float* bpx = a.bp[side == 3 ? bpx0 + 2 * comp : bpx0 + comp];
             const float Px = bpx[ap];
-            const float Pxn = ((1.0f - 0.5f * yx) * Px - dxc.dtdp * S1) / (1.0f + 0.5f * yx);
+            const float Pxn = ((1.0f - 0.5f * yx) * Px - dxc.dtdp * S1) * dxc.rh;
             bpx[ap] = Pxn;
             float* b1 = a.bu[base + 3 * comp + 0][plane];
             float* b1n = a.bu[base + 3 * comp + 0][nplane];
@@ -565,19 +569,19 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             const float f1 = kd * (F1 + 0.5f * (Pxn + Px));
             float n1;
             if (side == 2 && iz != 1)
-                n1 = ((2.0f - yx * yx) * u1 - (1.0f - yx) * u1m) / (1.0f + yx) + f1;
+                n1 = ((2.0f - yx * yx) * u1 - (1.0f - yx) * u1m) * dxc.r1 + f1;
             else
-                n1 = ((2.0f - yx * yx) * u1 - (1.0f - yx) * u1m + f1) / (1.0f + yx);
+                n1 = ((2.0f - yx * yx) * u1 - (1.0f - yx) * u1m + f1) * dxc.r1;
             const float u2 = b2[ap], u2m = b2n[ap];
-            const float n2 = ((2.0f - yx * yz) * u2 - (1.0f - 0.5f * (yx + yz)) * u2m + kd * F2) / (1.0f + 0.5f * (yx + yz));
+            const float n2 = ((2.0f - yx * yz) * u2 - (1.0f - 0.5f * (yx + yz)) * u2m + kd * F2) * r2;
             const float u3 = b3[ap], u3m = b3n[ap];
             float n3;
             if (side == 3) {
                 float* bpz = a.bp[9 + 2 * comp];
                 const float Pz = bpz[ap];
-                const float Pzn = ((1.0f - 0.5f * yz) * Pz - dzc.dtdp * S3) / (1.0f + 0.5f * yz);
+                const float Pzn = ((1.0f - 0.5f * yz) * Pz - dzc.dtdp * S3) * dzc.rh;
                 bpz[ap] = Pzn;
-                n3 = ((2.0f - yz * yz) * u3 - (1.0f - yz) * u3m + kd * (F3 + 0.5f * (Pzn + Pz))) / (1.0f + yz);
+                n3 = ((2.0f - yz * yz) * u3 - (1.0f - yz) * u3m + kd * (F3 + 0.5f * (Pzn + Pz))) * dzc.r1;
             } else {
                 n3 = fmaf(kd, F3, 2.0f * u3 - u3m);
             }
@@ -616,7 +620,7 @@ __device__ __forceinline__ int batch_member(const int* __restrict__ off, int n, 
 
 // The tiled kernel over every member of a batch: member s owns blocks edge_off[s] .. edge_off[s+1]-1.
 template <int NO>
-__global__ void __launch_bounds__(kThreads, 3) fdfk_step_batch_kernel(BatchTab t)
+__global__ void __launch_bounds__(kThreads, 4) fdfk_step_batch_kernel(BatchTab t)
 {
     const int s = batch_member(t.edge_off, t.n, blockIdx.x);
     if (!t.live[s]) return;

@@ -29,7 +29,15 @@ enum Strip { UXL_REG, UZL_REG, UXR_REG, UZR_REG, UXB_REG, UZB_REG,
 struct DampCol {   // per column (x) or row (z): d*dt and dt*d' for the PML
     float y;       // d * dt
     float dtdp;    // dt * dd/ds (signed along +x or +z)
+    float rh;      // 1 / (1 + y/2)
+    float r1;      // 1 / (1 + y)
 };
+
+// A DampCol from d*dt and dt*d' (the reciprocals formed in double, rounded once).
+inline DampCol make_damp(float y, float dtdp)
+{
+    return DampCol{y, dtdp, (float)(1.0 / (1.0 + 0.5 * (double)y)), (float)(1.0 / (1.0 + (double)y))};
+}
 
 struct StepArgs {
     // geometry (izt = 1, free surface on top)

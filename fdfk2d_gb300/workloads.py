@@ -194,6 +194,28 @@ def fk_inputs(w, ds=1e-3):
     return fp, bazs, _fk_model(left), _fk_model(right)
 
 
+def config3_events(n=64, seed=7):
+    """Plane-wave events of the batched workload (config 3, on the config-1 model): half P with
+    ray parameters uniform in 0.04-0.08 s/km, half S in 0.10-0.12 s/km, back-azimuths uniform in
+    0-360 degrees (taken along the profile), Ricker centre frequencies uniform in 0.5-1 Hz."""
+    rng = np.random.default_rng(seed)
+    ev = []
+    for i in range(n):
+        p_wave = i < n // 2
+        lo, hi = (0.04, 0.08) if p_wave else (0.10, 0.12)
+        ev.append(dict(p_wave=p_wave, rayp=float(rng.uniform(lo, hi)) * 1e-3, baz=float(rng.uniform(0.0, 360.0)),
+                       f0=float(np.float32(rng.uniform(0.5, 1.0)))))
+    return ev
+
+
+def event_inputs(w, ev, ds=1e-3):
+    """FK arguments (params, bazs, fk_left, fk_right) of one event on workload w."""
+    fp, bazs, fl, fr = fk_inputs(w, ds=ds)
+    fp = dict(fp, src_type=ev["p_wave"], rayp=ev["rayp"], f0=ev["f0"])
+    bazs = np.full_like(bazs, np.deg2rad(ev["baz"]))
+    return fp, bazs, fl, fr
+
+
 def check_shapes(w, strips):
     p = w["p"]
     shp = strip_shapes(p["nx"], p["nz"], p["nbd"], p["nt"])
