@@ -11,6 +11,8 @@ reference interface:
 * :func:`simulate` - the whole time loop in one call (host arrays in, seismograms out);
 * :class:`Batch` - many sessions advanced together (three launches per step for
   all of them, CUDA-graph replay);
+* :func:`run` - program FDFK2D itself: the reference's input folder in (:func:`read_input`),
+  SU seismograms out (:func:`write_su`), everything between on the GPU;
 * :class:`Server` - the serving loop: requests admitted by device-memory budget
   into a running batch (continuous batching), retired when done;
 * :func:`fk_background` / :func:`comput_background_wavefield` - the FK background
@@ -20,9 +22,11 @@ reference interface:
 There is no CPU fallback: if the CUDA library is missing or no GPU is
 visible, calls raise.
 """
-from .api import (Batch, FDFKError, FkParams, Params, Server, Session, session_device_bytes, STRIPS, BP, BU, comput_background_wavefield,
+from .api import (Batch, FDFKError, FkParams, Params, Server, Session, backazimuths, read_input, read_su, run,
+                  session_device_bytes, stable_dt, write_su, STRIPS, BP, BU, comput_background_wavefield,
                   fk_background, lib, lib_path, simulate, strip_shapes, pml_shapes, updatedispl, kernel_launches)
 
-__all__ = ["Batch", "FDFKError", "Server", "session_device_bytes", "FkParams", "Params", "Session", "STRIPS", "BP", "BU", "comput_background_wavefield",
+__all__ = ["Batch", "FDFKError", "Server", "backazimuths", "read_input", "read_su", "run", "session_device_bytes",
+           "stable_dt", "write_su", "FkParams", "Params", "Session", "STRIPS", "BP", "BU", "comput_background_wavefield",
            "fk_background", "lib", "lib_path", "simulate", "strip_shapes", "pml_shapes", "updatedispl",
            "kernel_launches"]

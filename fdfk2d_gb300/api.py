@@ -105,6 +105,7 @@ def lib():
         L.fdfk_session_create.argtypes = [C.POINTER(Params), C.c_void_p, C.POINTER(C.c_void_p)]
         L.fdfk_batch_destroy.restype = None
         L.fdfk_server_destroy.restype = None
+        L.fdfk_input_free.restype = None
         L.fdfk_session_device_bytes.restype = C.c_longlong
         for name in ("fdfk_session_set_stream", "fdfk_session_advance", "fdfk_session_synchronize",
                      "fdfk_session_step_index", "fdfk_session_destroy", "fdfk_session_upload_background",
@@ -115,7 +116,8 @@ def lib():
                      "fdfk_batch_create", "fdfk_batch_add", "fdfk_batch_remove", "fdfk_batch_set_graph_chunk",
                      "fdfk_batch_advance", "fdfk_batch_synchronize", "fdfk_batch_live", "fdfk_batch_size",
                      "fdfk_server_create", "fdfk_server_submit", "fdfk_server_pump", "fdfk_server_request",
-                     "fdfk_server_get_stats"):
+                     "fdfk_server_get_stats", "fdfk_input_read", "fdfk_backazimuths", "fdfk_stable_dt",
+                     "fdfk_write_su", "fdfk_run", "fdfk_session_snapshot"):
             getattr(L, name).restype = C.c_int if name != "fdfk_session_destroy" else None
         _lib = L
     return _lib
@@ -242,6 +244,14 @@ class Session:
         sz = np.zeros_like(sx, order="F")
         _check(lib().fdfk_session_download_seismograms(self._h, _f32(sx, "seisx"), _f32(sz, "seisz")))
         return sx, sz
+
+    def snapshot(self):
+        """Level 2 (u^{n-1}) of rows 1..nz, columns 1..nx as (nz, nx) arrays (ux, uz)."""
+        nz, nx = int(self.p["nz"]), int(self.p["nx"])
+        ux = np.zeros((nz, nx), np.float32, order="F")
+        uz = np.zeros((nz, nx), np.float32, order="F")
+        _check(lib().fdfk_session_snapshot(self._h, _f32(ux, "ux"), _f32(uz, "uz")))
+        return ux, uz
 
     def seismogram_range(self, first: int, count: int, outx=None, outz=None):
         """Samples [first, first+count) of every receiver, arrays of shape (count, nrcv)."""
@@ -402,6 +412,83 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class InputFolder(C.Structure):
+    """fdfk_input: the parsed input folder of FDFK2D (src/Input.f90)."""
+    _fields_ = [("norder", C.c_int), ("nx", C.c_int), ("nz", C.c_int), ("npml", C.c_int), ("izt", C.c_int),
+                ("is_PML_top", C.c_int), ("outsnap", C.c_int), ("nstep", C.c_int), ("src_type", C.c_int),
+                ("nrcv", C.c_int), ("nlayer_left", C.c_int), ("nlayer_right", C.c_int),
+                ("negative_velocity", C.c_int), ("x0", C.c_float), ("z0", C.c_float), ("dx", C.c_float),
+                ("dz", C.c_float), ("tmax", C.c_float), ("tstp", C.c_float), ("f0", C.c_float), ("ds", C.c_float),
+                ("dt", C.c_double), ("rayp", C.c_double), ("evla", C.c_double), ("evlo", C.c_double),
+                ("lat_org", C.c_double), ("lon_org", C.c_double), ("az_org", C.c_double),
+                ("rx", C.POINTER(C.c_float)), ("rz", C.POINTER(C.c_float)), ("fk_left", C.POINTER(C.c_float)),
+                ("fk_right", C.POINTER(C.c_float)), ("c", C.POINTER(C.c_float))]
+
+
+def read_input(inpath: str, inpar: str, write_model_copies: bool = False) -> dict:
+    """Parse an FDFK2D input folder; returns scalars plus rx, rz, fk_left, fk_right (4, nl), c (3, NZ, NX)."""
+    L = lib()
+    inp = InputFolder()
+    rc = L.fdfk_input_read(inpath.encode(), inpar.encode(), C.c_int(1 if write_model_copies else 0), C.byref(inp))
+    try:
+        _check(rc)
+        out = {k: getattr(inp, k) for k, t in InputFolder._fields_ if not k in ("rx", "rz", "fk_left", "fk_right", "c")}
+        NX, NZ = inp.nx + 2 * inp.npml, inp.nz + inp.npml - inp.izt + 1
+        arr = lambda ptr, n: np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+        out["rx"] = arr(inp.rx, inp.nrcv)
+        out["rz"] = arr(inp.rz, inp.nrcv)
+        out["fk_left"] = np.asfortranarray(arr(inp.fk_left, 4 * inp.nlayer_left).reshape(inp.nlayer_left, 4).T)
+        out["fk_right"] = np.asfortranarray(arr(inp.fk_right, 4 * inp.nlayer_right).reshape(inp.nlayer_right, 4).T)
+        out["c"] = np.asfortranarray(arr(inp.c, 3 * NX * NZ).reshape(NX, NZ, 3).transpose(2, 1, 0))
+        return out
+    finally:
+        L.fdfk_input_free(C.byref(inp))
+
+
+def backazimuths(lat_org, lon_org, az_org, evla, evlo, coordx) -> np.ndarray:
+    """Back-azimuths (rad) at profile coordinates, minus the profile azimuth (src/coord_transform.f90)."""
+    x = np.ascontiguousarray(coordx, np.float32)
+    out = np.zeros(x.size, np.float64)
+    _check(lib().fdfk_backazimuths(C.c_double(lat_org), C.c_double(lon_org), C.c_double(az_org), C.c_double(evla),
+                                   C.c_double(evlo), C.c_int(x.size), x.ctypes.data_as(C.c_void_p),
+                                   out.ctypes.data_as(C.c_void_p)))
+    return out
+
+
+def stable_dt(norder: int, nx: int, nz: int, npml: int, dx: float, dz: float, c) -> float:
+    """check_stability's stable dt (src/Submain.f90:118-164)."""
+    v = C.c_double()
+    _check(lib().fdfk_stable_dt(C.c_int(norder), C.c_int(nx), C.c_int(nz), C.c_int(npml), C.c_float(dx),
+                                C.c_float(dz), _f32(c, "c"), C.byref(v)))
+    return v.value
+
+
+def write_su(path: str, data, head58: int, head59: int):
+    """SU file from data (ns, ntr), one trace per column."""
+    d = np.asfortranarray(data, np.float32)
+    _check(lib().fdfk_write_su(path.encode(), C.c_int(d.shape[1]), C.c_int(d.shape[0]), d.ctypes.data_as(C.c_void_p),
+                               C.c_int(head58), C.c_int(head59)))
+
+
+def read_su(path: str, ns: int):
+    """(headers (ntr, 120) int16, data (ns, ntr) float32) of an SU file of ns-sample traces."""
+    raw = np.fromfile(path, np.uint8)
+    rec = 240 + 4 * ns
+    if raw.size % rec:
+        raise ValueError(f"{path}: size is not a whole number of {ns}-sample traces")
+    ntr = raw.size // rec
+    r = raw.reshape(ntr, rec)
+    heads = r[:, :240].copy().view(np.int16)
+    data = np.asfortranarray(r[:, 240:].copy().view(np.float32).T)
+    return heads, data
+
+
+def run(inpath: str, inpar: str, outpath: str, fsis: str = "seis", write_model_copies: bool = True):
+    """Program FDFK2D on the GPU: input folder in, <outpath>/<fsis>x.su and z.su out."""
+    _check(lib().fdfk_run(inpath.encode(), inpar.encode(), outpath.encode(), fsis.encode(),
+                          C.c_int(1 if write_model_copies else 0)))
 
 
 def simulate(p: dict, c: np.ndarray, strips: dict, rx, rz, x0: float, z0: float, nstp: int, nsis: int):

@@ -670,6 +670,25 @@ int fdfk_session_download_state(fdfk_session* s, float* ux, float* uz, float* co
     return FDFK_OK;
 }
 
+int fdfk_session_snapshot(fdfk_session* s, float* ux, float* uz)
+{
+    if (!s || !ux || !uz) return fail(FDFK_EINVAL, "NULL argument");
+    if (s->batch) {
+        const int rb = fdfk_batch_synchronize(s->batch);
+        if (rb) return rb;
+    }
+    // level 2 = the plane not holding u^n; rows 1..nz of columns 1..nx
+    const int o = s->cur ^ 1;
+    const size_t first = (size_t)s->ldz * s->p.npml;
+    const size_t pitch = (size_t)s->ldz * sizeof(float);
+    CK(cudaMemcpy2DAsync(ux, s->p.nz * sizeof(float), s->ux[o] + first, pitch, s->p.nz * sizeof(float), s->p.nx,
+                         cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpy2DAsync(uz, s->p.nz * sizeof(float), s->uz[o] + first, pitch, s->p.nz * sizeof(float), s->p.nx,
+                         cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return FDFK_OK;
+}
+
 void fdfk_session_destroy(fdfk_session* s)
 {
     if (s && s->batch) fdfk_batch_remove(s->batch, s);

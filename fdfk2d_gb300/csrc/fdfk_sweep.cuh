@@ -9,6 +9,9 @@
 // sampling (loadseis, src/Submain.f90:33-116) runs in the same launch on
 // extra CTAs, reading the level that the step itself never writes.
 #pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
 #include <cstdint>
 
 namespace fdfk {

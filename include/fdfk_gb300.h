@@ -128,7 +128,67 @@ int fdfk_session_upload_state(fdfk_session* s, const float* ux, const float* uz,
                               const float* const bu[24], int it);
 int fdfk_session_download_state(fdfk_session* s, float* ux, float* uz, float* const bp[12], float* const bu[24]);
 
+/*
+ * Snapshot of level 2 (u^{n-1} before the next step) of rows 1..nz, columns
+ * 1..nx into host arrays (nz, nx), z fastest, as the snapshot files of
+ * src/FDFK2D.f90:467-494 hold.  Waits for the session stream.
+ */
+int fdfk_session_snapshot(fdfk_session* s, float* ux, float* uz);
+
 void fdfk_session_destroy(fdfk_session* s);
+
+/*
+ * The input folder of FDFK2D (src/Input.f90): the inpar file names, in
+ * order, the FD model, source, receiver, left and right FK model, Vp and Vs
+ * model files.  Text files are read with Fortran list-directed rules; the
+ * Vp/Vs models are SU files of nx + 2 npml traces (240-byte headers) of
+ * nz + npml - izt + 1 samples.  fdfk_input_read fills *in (arrays allocated
+ * here, released by fdfk_input_free) and, when write_model_copies is set,
+ * writes <model>_without_pml.su next to the input models as the reference
+ * does (src/Input.f90:311-321).
+ */
+typedef struct fdfk_input {
+    int norder;                 /* half order, after the reference's reduction to npml */
+    int nx, nz, npml, izt;
+    int is_PML_top, outsnap, nstep, src_type;
+    int nrcv, nlayer_left, nlayer_right;
+    int negative_velocity;      /* a negative vp or vs was read (the reference prints an error) */
+    float x0, z0, dx, dz, tmax, tstp, f0, ds;
+    double dt, rayp;            /* rayp in s/m (read in s/deg) */
+    double evla, evlo, lat_org, lon_org, az_org;
+    float* rx;
+    float* rz;
+    float* fk_left;             /* (4, nlayer_left): z_top, vp, vs, rho */
+    float* fk_right;
+    float* c;                   /* c(1:3, NZ, NX) = rho, lambda, mu with rho = (vp + 980) / 2.76 */
+} fdfk_input;
+
+int fdfk_input_read(const char* inpath, const char* inparfile, int write_model_copies, fdfk_input* in);
+void fdfk_input_free(fdfk_input* in);
+
+/* compute_backazimuth_grids (src/coord_transform.f90) minus the profile azimuth
+ * (src/FDFK2D.f90:387): back-azimuths (rad) at profile coordinates coordx[n]. */
+int fdfk_backazimuths(double lat_org, double lon_org, double az_org, double evla, double evlo, int n,
+                      const float* coordx, double* bazs);
+
+/* check_stability (src/Submain.f90:118-164): the largest stable dt for c. */
+int fdfk_stable_dt(int norder, int nx, int nz, int npml, float dx, float dz, const float* c, double* dt_stable);
+
+/* An SU file of ntr traces of ns samples (data trace-major, sample fastest),
+ * header words 58 and 59 (1-based, int16) set as the reference sets them. */
+int fdfk_write_su(const char* path, int ntr, int ns, const float* data, int head58, int head59);
+
+/*
+ * Program FDFK2D (src/FDFK2D.f90) on the GPU: read the input folder, check
+ * stability, compute the back-azimuths of the grid, the FK background on the
+ * GPU, the time loop with receiver sampling (and snapshots into
+ * <outpath>/snapshots/ when the FD model asks for them), project the radial
+ * component and write <outpath>/<fsis>x.su and <fsis>z.su ("seis" when fsis
+ * is NULL or empty).  Where the reference asks on stdin whether to continue
+ * (profile more than 30 degrees off the back-azimuth) this prints a warning
+ * and continues.
+ */
+int fdfk_run(const char* inpath, const char* inparfile, const char* outpath, const char* fsis, int write_model_copies);
 
 /*
  * Batches: many solves advanced together (events of one model, or models of

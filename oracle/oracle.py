@@ -83,6 +83,16 @@ def fd_coef2(norder):
     return _coef("fdfk_op_fd_coef2", norder)
 
 
+def dt_stable(nx, nz, npml, izt, norder, dx, dz, c):
+    """check_stability's stable dt (src/Submain.f90:118-164), restated."""
+    L = lib()
+    L.fdfk_op_dt_stable.restype = C.c_float
+    coef2 = fd_coef2(norder)
+    return float(L.fdfk_op_dt_stable(C.c_int(nx), C.c_int(nz), C.c_int(npml), C.c_int(izt), C.c_int(norder),
+                                     C.c_float(dx), C.c_float(dz), _ptr(coef2, np.float64),
+                                     _ptr(np.asfortranarray(c, np.float32))))
+
+
 def updatedispl(p, strips, c, coef0, coef1, ux, uz, bp, bu, it):
     L = lib()
     sp = (C.c_void_p * 12)(*[_ptr(strips[k]) for k in STRIPS])

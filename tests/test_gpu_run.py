@@ -1,0 +1,87 @@
+"""GPU: program FDFK2D through fdfk_run - the reference's input folder in, SU seismograms out -
+against the oracle pipeline on the same inputs (FK restatement, restated time loop, radial
+projection)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from io_folder import write_folder
+
+import fk_oracle
+
+pytestmark = pytest.mark.gpu
+
+TRACE_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def F():
+    import fdfk2d_gb300 as F
+    from fdfk2d_gb300 import build
+    build.build()
+    F.lib()
+    return F
+
+
+def _oracle_pipeline(F, oracle_lib, inp):
+    d = F.read_input(inp, "inpar.dat")
+    nx, nz, npml, dt = d["nx"], d["nz"], d["npml"], d["dt"]
+    nt = int(round(float(d["tmax"]) / dt))
+    nstp = int(round(max(float(d["tstp"]), dt) / dt))
+    nsis = nt // nstp
+    c = d["c"]
+    vpml = float(np.sqrt((c[1] + 2 * c[2]) / c[0]).max())
+    p = dict(norder=d["norder"], nx=nx, nz=nz, npml=npml, nbd=2 * d["norder"] - 1, nt=nt, dx=d["dx"], dz=d["dz"],
+             dt=dt, vpml=vpml, npower=2, R0=1e-3, izt=1)
+    coordx = (np.float32(d["x0"]) + (np.arange(1 - npml, nx + npml + 1) - 1).astype(np.float32) * np.float32(d["dx"]))
+    bazs = F.backazimuths(d["lat_org"], d["lon_org"], d["az_org"], d["evla"], d["evlo"], coordx)
+    fp = dict(nx=nx, nz=nz, npml=npml, nbd=p["nbd"], nt=nt, dt=dt, dx=d["dx"], dz=d["dz"], f0=d["f0"], ds=d["ds"],
+              rayp=d["rayp"], src_type=bool(d["src_type"]))
+    strips = fk_oracle.background(fp, bazs, d["fk_left"], d["fk_right"], x0=float(d["x0"]), z0=float(d["z0"]))
+    sx, sz = oracle_lib.simulate(p, strips, c, d["rx"], d["rz"], d["x0"], d["z0"], nstp, nsis)
+    rb = F.backazimuths(d["lat_org"], d["lon_org"], d["az_org"], d["evla"], d["evlo"], d["rx"])
+    sx = (sx.astype(np.float64) * np.cos(rb)[None, :]).astype(np.float32)
+    return sx, sz, nsis, np.float32(nstp * dt)
+
+
+def test_run_matches_oracle_pipeline(F, oracle_lib, tmp_path):
+    inp, out = str(tmp_path / "in"), str(tmp_path / "out")
+    write_folder(inp)
+    os.makedirs(out)
+    F.run(inp, "inpar.dat", out, "seis")
+    ox, oz, nsis, tstp = _oracle_pipeline(F, oracle_lib, inp)
+    hx, gx = F.read_su(os.path.join(out, "seisx.su"), nsis + 1)
+    hz, gz = F.read_su(os.path.join(out, "seisz.su"), nsis + 1)
+    assert gx.shape == ox.shape and gz.shape == oz.shape
+    assert (hx[:, 57] == nsis + 1).all() and (hx[:, 58] == int(tstp * np.float32(1e6))).all()
+    assert np.abs(oz).max() > 0
+    assert rel_l2(gx, ox) < TRACE_TOL and rel_l2(gz, oz) < TRACE_TOL
+    assert os.path.exists(os.path.join(inp, "vp_without_pml.su"))
+
+
+def test_run_writes_snapshots_of_level_two(F, tmp_path):
+    inp, out = str(tmp_path / "in"), str(tmp_path / "out")
+    write_folder(inp, outsnap=True, nstep=40, tmax=1.2)
+    os.makedirs(out)
+    F.run(inp, "inpar.dat", out, "s", write_model_copies=False)
+    names = sorted(os.listdir(os.path.join(out, "snapshots")))
+    assert names == ["00040ux.su", "00040uz.su", "00080ux.su", "00080uz.su"]
+    h, snap = F.read_su(os.path.join(out, "snapshots", "00080uz.su"), 24)
+    assert snap.shape == (24, 40) and (h[:, 57] == 24).all() and (h[:, 58] == 250).all()
+    # the same state from a session stepped to time index 80
+    d = F.read_input(inp, "inpar.dat")
+    c = d["c"]
+    vpml = float(np.sqrt((c[1] + 2 * c[2]) / c[0]).max())
+    p = dict(norder=3, nx=40, nz=24, npml=8, nbd=5, nt=80, dx=250.0, dz=250.0, dt=0.015, vpml=vpml)
+    coordx = (np.arange(1 - 8, 40 + 8 + 1) - 1).astype(np.float32) * np.float32(250.0)
+    bazs = F.backazimuths(d["lat_org"], d["lon_org"], d["az_org"], d["evla"], d["evlo"], coordx)
+    fp = dict(nx=40, nz=24, npml=8, nbd=5, nt=80, dt=0.015, dx=250.0, dz=250.0, f0=2.0, ds=1e-3, rayp=d["rayp"],
+              src_type=True)
+    with F.Session(p, c) as s:                   # tmax 1.2 s = 80 steps: the run's record length
+        s.fk_background(fp, bazs, d["fk_left"], d["fk_right"])
+        s.advance(80)
+        sx, sz = s.snapshot()
+    assert np.abs(snap).max() > 0
+    np.testing.assert_array_equal(snap, sz)
