@@ -245,6 +245,7 @@ def main():
     ap.add_argument("--workload", default="config2", choices=["config2", "config1"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fk-full", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--batch-events", type=int, default=64, help="config-3 events (0: skip batched and serving)")
     ap.add_argument("--seq-sample", type=int, default=8, help="sequential solves timed for the comparison")
     ap.add_argument("--serve-requests", type=int, default=192, help="config-5 requests (0: skip serving)")
@@ -298,7 +299,13 @@ def main():
     K2 = min(K, 200)
     q = dict(p, nt=Wm + K + K2 - 1)
     fkp, bazs, fk_left, fk_right = WL.fk_inputs(dict(w, p=q))
+    tuning = None
+    if not args.no_autotune:
+        seg, run, ms_tuned = F.autotune(p, w["c"], steps=20)
+        tuning = {"seg_len": seg, "pml_run": run, "ms_per_step_in_tuner": round(ms_tuned, 4)}
     sess = F.Session(q, w["c"], stream=stream.cuda_stream)
+    if tuning:
+        sess.set_tuning(tuning["seg_len"], tuning["pml_run"])
     sess.fk_background(fkp, bazs, fk_left, fk_right)
     sess.set_receivers(w["rx"], w["rz"], w["x0"], w["z0"], 1, q["nt"])
     sess.advance(Wm)
@@ -402,6 +409,8 @@ def main():
                              "whole_step_equiv_gbs": round(step_equiv, 1),
                              "whole_step_frac": round(step_equiv / peak, 4)},
                 "cpu_baseline": cpu, "clocks": clk}
+        if tuning:
+            line["config"]["tuning"] = dict(tuning, note="launch shapes picked by fdfk_autotune")
         if extra:
             line.update(extra)
         if fk_ms is not None:

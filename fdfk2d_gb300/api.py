@@ -117,7 +117,8 @@ def lib():
                      "fdfk_batch_advance", "fdfk_batch_synchronize", "fdfk_batch_live", "fdfk_batch_size",
                      "fdfk_server_create", "fdfk_server_submit", "fdfk_server_pump", "fdfk_server_request",
                      "fdfk_server_get_stats", "fdfk_input_read", "fdfk_backazimuths", "fdfk_stable_dt",
-                     "fdfk_write_su", "fdfk_run", "fdfk_session_snapshot"):
+                     "fdfk_write_su", "fdfk_run", "fdfk_session_snapshot", "fdfk_session_set_tuning",
+                     "fdfk_session_get_tuning", "fdfk_autotune"):
             getattr(L, name).restype = C.c_int if name != "fdfk_session_destroy" else None
         _lib = L
     return _lib
@@ -244,6 +245,15 @@ class Session:
         sz = np.zeros_like(sx, order="F")
         _check(lib().fdfk_session_download_seismograms(self._h, _f32(sx, "seisx"), _f32(sz, "seisz")))
         return sx, sz
+
+    def set_tuning(self, seg_len: int = 0, pml_run: int = 0):
+        """Launch shapes (results do not change): fast-path segment length, absorbing-layer tile length."""
+        _check(lib().fdfk_session_set_tuning(self._h, C.c_int(int(seg_len)), C.c_int(int(pml_run))))
+
+    def tuning(self):
+        a, b = C.c_int(), C.c_int()
+        _check(lib().fdfk_session_get_tuning(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def snapshot(self):
         """Level 2 (u^{n-1}) of rows 1..nz, columns 1..nx as (nz, nx) arrays (ux, uz)."""
@@ -445,6 +455,14 @@ def read_input(inpath: str, inpar: str, write_model_copies: bool = False) -> dic
         return out
     finally:
         L.fdfk_input_free(C.byref(inp))
+
+
+def autotune(p: dict, c, steps: int = 20):
+    """Fastest (seg_len, pml_run) for sessions of p and c, and its ms per step (fdfk_autotune)."""
+    prm = Params.from_dict(p)
+    a, b, ms = C.c_int(), C.c_int(), C.c_float()
+    _check(lib().fdfk_autotune(C.byref(prm), _f32(c, "c"), C.c_int(int(steps)), C.byref(a), C.byref(b), C.byref(ms)))
+    return a.value, b.value, ms.value
 
 
 def backazimuths(lat_org, lon_org, az_org, evla, evlo, coordx) -> np.ndarray:

@@ -161,7 +161,7 @@ int rebuild(fdfk_batch* b)
         d.nrcv = s->nrcv; d.nstp = s->nstp; d.nsis = s->nsis; d.isis = s->isis; d.istp = s->istp;
         d.live = s->it <= s->p.nt;
         dyn[i] = d;
-        const int nsb = s->nrcv > 0 ? (s->nrcv + kThreads - 1) / kThreads : 0;
+        const int nsb = sample_blocks(s->nrcv);
         eoff[i + 1] = eoff[i] + a.n_tiles + nsb;
         moff[i + 1] = moff[i] + (m.n_bands * m.n_segs + 3) / 4;
         smem = std::max(smem, step_smem_for(a));

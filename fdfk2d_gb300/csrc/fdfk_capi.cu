@@ -670,6 +670,87 @@ int fdfk_session_download_state(fdfk_session* s, float* ux, float* uz, float* co
     return FDFK_OK;
 }
 
+int fdfk_session_set_tuning(fdfk_session* s, int seg_len, int pml_run)
+{
+    if (!s) return fail(FDFK_EINVAL, "session is NULL");
+    if (s->batch) return fail(FDFK_ESTATE, "the session is a member of a batch");
+    if ((seg_len != 0 && (seg_len < 8 || seg_len > 1024)) || (pml_run != 0 && (pml_run < 8 || pml_run > 64)))
+        return fail(FDFK_EINVAL, "segment length must be 8..1024 and tile length 8..64 (0 keeps the current)");
+    if (seg_len && s->march.n_bands > 0) {
+        s->march.seg_len = seg_len;
+        s->march.n_segs = (s->p.nx + seg_len - 1) / seg_len;
+    }
+    if (pml_run) {
+        s->pml_run = pml_run;
+        plan_tiles(s->base, s->march.n_bands > 0, pml_run);
+    }
+    return FDFK_OK;
+}
+
+int fdfk_session_get_tuning(const fdfk_session* s, int* seg_len, int* pml_run)
+{
+    if (!s || !seg_len || !pml_run) return fail(FDFK_EINVAL, "NULL argument");
+    *seg_len = s->march.n_bands > 0 ? s->march.seg_len : 0;
+    *pml_run = s->pml_run;
+    return FDFK_OK;
+}
+
+int fdfk_autotune(const fdfk_params* p, const float* c, int steps, int* seg_len, int* pml_run, float* ms_per_step)
+{
+    if (!p || !c || !seg_len || !pml_run || steps < 1) return fail(FDFK_EINVAL, "bad argument");
+    const int segs[] = {16, 24, 32, 48, 64, 96};
+    const int runs[] = {16, 24, 32, 48};
+    const int trials = 6 + 4;
+    fdfk_params q = *p;
+    q.nt = trials * (steps + 2) + 1;
+    fdfk_session* s = nullptr;
+    int rc = fdfk_session_create(&q, c, &s);
+    if (rc) return rc;
+    struct Guard {
+        fdfk_session* s;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        ~Guard()
+        {
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            fdfk_session_destroy(s);
+        }
+    } g{s};
+    // a zero background: the timing of a step does not depend on the values
+    for (int k = 0; k < NSTRIP; ++k)
+        CK(cudaMemsetAsync(s->strip[k], 0, strip_elems(q, k) * (size_t)(q.nt + 1) * sizeof(float), s->stream));
+    for (int t = 0; t <= q.nt; ++t) s->have_bg[t] = 1;
+    CK(cudaEventCreate(&g.e0));
+    CK(cudaEventCreate(&g.e1));
+    auto time_it = [&](int seg, int run, float& ms) -> int {
+        int r = fdfk_session_set_tuning(s, seg, run);
+        if (r) return r;
+        if ((r = fdfk_session_advance(s, 2))) return r;   // warm-up (first launches of a shape)
+        CK(cudaEventRecord(g.e0, s->stream));
+        if ((r = fdfk_session_advance(s, steps))) return r;
+        CK(cudaEventRecord(g.e1, s->stream));
+        CK(cudaEventSynchronize(g.e1));
+        CK(cudaEventElapsedTime(&ms, g.e0, g.e1));
+        ms /= steps;
+        return FDFK_OK;
+    };
+    int best_seg = s->march.n_bands > 0 ? s->march.seg_len : 0, best_run = s->pml_run;
+    float best = 1e30f, ms = 0.f;
+    if (s->march.n_bands > 0)
+        for (int seg : segs) {
+            if ((rc = time_it(seg, best_run, ms))) return rc;
+            if (ms < best) { best = ms; best_seg = seg; }
+        }
+    for (int run : runs) {
+        if ((rc = time_it(best_seg, run, ms))) return rc;
+        if (ms < best) { best = ms; best_run = run; }
+    }
+    *seg_len = best_seg;
+    *pml_run = best_run;
+    if (ms_per_step) *ms_per_step = best;
+    return FDFK_OK;
+}
+
 int fdfk_session_snapshot(fdfk_session* s, float* ux, float* uz)
 {
     if (!s || !ux || !uz) return fail(FDFK_EINVAL, "NULL argument");

@@ -39,6 +39,7 @@ struct fdfk_session {
     fdfk::StepArgs base{};
     fdfk::MarchArgs march{};
     fdfk_batch* batch = nullptr;   // set while the session is a member of a batch
+    int pml_run = fdfk::kPmlRun;   // absorbing-layer tile length (tunable)
 };
 
 namespace fdfk {

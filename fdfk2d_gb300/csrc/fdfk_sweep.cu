@@ -166,30 +166,41 @@ __device__ __forceinline__ double delta_weight(double x)
     return 0.0;
 }
 
+// One warp per receiver: the lanes share the (at most) 7 x 7 grid points, each forms its weight
+// and product in FP64, and a shuffle reduction sums them (FP64).
 __device__ void sample_receivers(const StepArgs& a, int blk)
 {
-    int r = blk * kThreads + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int r = blk * (kThreads / 32) + (threadIdx.x >> 5);
     if (r >= a.nrcv) return;
     const float* ux = a.ux[a.cur];
     const float* uz = a.uz[a.cur];
-    float rx = a.rx[r], rz = a.rz[r];
-    int irx = (int)floorf((rx - a.x0) / a.dx) + 1;
-    int irz = (int)floorf((rz - a.z0) / a.dz) + 1;
+    const float rx = a.rx[r], rz = a.rz[r];
+    const int irx = (int)floorf((rx - a.x0) / a.dx) + 1;
+    const int irz = (int)floorf((rz - a.z0) / a.dz) + 1;
+    const int xlo = max(1 - a.npml, irx - 3), xhi = min(a.nx + a.npml, irx + 3);
+    const int zlo = max(1, irz - 3), zhi = min(a.nz + a.npml, irz + 3);
     double sx = 0.0, sz = 0.0;
-    for (int ix = max(1 - a.npml, irx - 3); ix <= min(a.nx + a.npml, irx + 3); ++ix) {
-        double x = fabs((double)__fadd_rn(a.x0, __fmul_rn((float)(ix - 1), a.dx)) - (double)rx) / (double)a.dx;
-        double bx = delta_weight(x);
-        for (int iz = max(1, irz - 3); iz <= min(a.nz + a.npml, irz + 3); ++iz) {
-            double z = fabs((double)__fadd_rn(a.z0, __fmul_rn((float)(iz - 1), a.dz)) - (double)rz) / (double)a.dz;
-            double w = bx * delta_weight(z);
-            size_t g = gidx(a, iz, ix);
-            sx += w * (double)ux[g];
-            sz += w * (double)uz[g];
-        }
+    for (int q = lane; q < 49; q += 32) {
+        const int ix = irx - 3 + q / 7, iz = irz - 3 + q % 7;
+        if (ix < xlo || ix > xhi || iz < zlo || iz > zhi) continue;
+        const double x = fabs((double)__fadd_rn(a.x0, __fmul_rn((float)(ix - 1), a.dx)) - (double)rx) / (double)a.dx;
+        const double z = fabs((double)__fadd_rn(a.z0, __fmul_rn((float)(iz - 1), a.dz)) - (double)rz) / (double)a.dz;
+        const double w = delta_weight(x) * delta_weight(z);
+        const size_t g = gidx(a, iz, ix);
+        sx += w * (double)ux[g];
+        sz += w * (double)uz[g];
     }
-    size_t o = (size_t)a.sample_index + (size_t)a.nsamp * (size_t)r;
-    a.seisx[o] = (float)sx;
-    a.seisz[o] = (float)sz;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_down_sync(0xffffffffu, sx, o);
+        sz += __shfl_down_sync(0xffffffffu, sz, o);
+    }
+    if (lane == 0) {
+        const size_t o = (size_t)a.sample_index + (size_t)a.nsamp * (size_t)r;
+        a.seisx[o] = (float)sx;
+        a.seisz[o] = (float)sz;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -674,9 +685,12 @@ static cudaError_t launch_no(const StepArgs& a, int n_sample_blocks, cudaStream_
     return cudaGetLastError();
 }
 
+// Receiver-sampling blocks appended to a tiled launch (one warp per receiver).
+int sample_blocks(int nrcv) { return nrcv > 0 ? (nrcv + kThreads / 32 - 1) / (kThreads / 32) : 0; }
+
 cudaError_t launch_step(const StepArgs& a, cudaStream_t s)
 {
-    int nsb = a.nrcv > 0 ? (a.nrcv + kThreads - 1) / kThreads : 0;
+    int nsb = sample_blocks(a.nrcv);
     switch (a.norder) {
     case 1: return launch_no<1>(a, nsb, s);
     case 2: return launch_no<2>(a, nsb, s);
@@ -737,16 +751,17 @@ size_t step_smem_for(const StepArgs& a)
 // Tile shapes and counts of the tiled kernel.  band_top: the fast path covers rows below
 // int_rows, so the interior tiles are flat kBandTZ x kBandTX tiles of the top band.  The
 // absorbing layers are cut into tiles whose thickness divides npml evenly (at most kPmlTile)
-// and kPmlRun cells along the layer.
-void plan_tiles(StepArgs& a, bool band_top)
+// and pml_run cells (kPmlRun when not tuned) along the layer.
+void plan_tiles(StepArgs& a, bool band_top, int pml_run)
 {
+    if (pml_run < 8) pml_run = kPmlRun;
     auto cdiv = [](int x, int y) { return (x + y - 1) / y; };
     const int nt = cdiv(a.npml, kPmlTile);
     const int th = cdiv(a.npml, nt);
     a.tdz[0] = band_top ? kBandTZ : kTZ;
     a.tdx[0] = band_top ? kBandTX : kTX;
-    a.tdz[1] = kPmlRun; a.tdx[1] = th;
-    a.tdz[2] = th; a.tdx[2] = kPmlRun;
+    a.tdz[1] = pml_run; a.tdx[1] = th;
+    a.tdz[2] = th; a.tdx[2] = pml_run;
     a.tiles_int_z = cdiv(a.int_rows, a.tdz[0]);
     a.tiles_int_x = cdiv(a.nx, a.tdx[0]);
     a.tiles_l_z = cdiv(a.nz, a.tdz[1]);

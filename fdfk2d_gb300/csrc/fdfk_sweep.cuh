@@ -93,10 +93,12 @@ struct MarchArgs {
 };
 
 // Tile shapes and counts of fdfk_step_kernel for a (fdfk_sweep.cu); needs nx, nz, npml, NX, int_rows.
-void plan_tiles(StepArgs& a, bool band_top);
+void plan_tiles(StepArgs& a, bool band_top, int pml_run = kPmlRun);
 
 // Dynamic shared memory of a's tiled launch.
 size_t step_smem_for(const StepArgs& a);
+// Receiver-sampling blocks a tiled launch appends for nrcv receivers.
+int sample_blocks(int nrcv);
 
 // Device-side per-member state of a batch (advanced by fdfk_batch_bump before every step).
 struct BatchDyn {

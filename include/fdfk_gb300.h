@@ -129,6 +129,22 @@ int fdfk_session_upload_state(fdfk_session* s, const float* ux, const float* uz,
 int fdfk_session_download_state(fdfk_session* s, float* ux, float* uz, float* const bp[12], float* const bu[24]);
 
 /*
+ * Launch shapes of a session (results are identical for every choice): the
+ * fast path's segment length in columns (8..1024) and the absorbing-layer
+ * tile length along the layer (8..64); 0 keeps the current value.
+ */
+int fdfk_session_set_tuning(fdfk_session* s, int seg_len, int pml_run);
+int fdfk_session_get_tuning(const fdfk_session* s, int* seg_len, int* pml_run);
+
+/*
+ * Autotuner: times candidate launch shapes (segment lengths 16..96, tile
+ * lengths 16..48) for sessions of parameters p and material c on a scratch
+ * session (zero state and background, `steps` timed steps per candidate,
+ * CUDA events) and returns the fastest, for fdfk_session_set_tuning.
+ */
+int fdfk_autotune(const fdfk_params* p, const float* c, int steps, int* seg_len, int* pml_run, float* ms_per_step);
+
+/*
  * Snapshot of level 2 (u^{n-1} before the next step) of rows 1..nz, columns
  * 1..nx into host arrays (nz, nx), z fastest, as the snapshot files of
  * src/FDFK2D.f90:467-494 hold.  Waits for the session stream.

@@ -197,3 +197,22 @@ def test_interior_fast_path_matches_tiled_path_and_oracle(F, oracle_lib, norder)
                            {k: v.copy(order="F") for k, v in bu.items()}, 0)
     assert max_rel(mx, ox) < STEP_TOL
     assert max_rel(mz, oz) < STEP_TOL
+
+
+def test_tuning_changes_no_result(F):
+    """Every launch shape gives the same bits (the autotuner may pick any of them)."""
+    d = load_npz("loop_layered")
+    p = dict(d["p"])
+    strips = {k: d[k] for k in F.STRIPS}
+    seg, run, ms = F.autotune(p, d["c"], steps=5)
+    assert seg >= 16 and 16 <= run <= 48 and ms > 0
+    out = []
+    for tune in ((0, 0), (16, 16), (96, 48), (seg, run)):
+        with F.Session(p, d["c"]) as s:
+            s.set_tuning(*tune)
+            s.upload_background(strips)
+            s.set_receivers(d["rx"], d["rz"], 0.0, 0.0, int(d["nstp"]), int(d["nsis"]))
+            s.advance(p["nt"] + 1)
+            out.append(s.seismograms())
+    for sx, sz in out[1:]:
+        assert np.array_equal(sx, out[0][0]) and np.array_equal(sz, out[0][1])
