@@ -9,9 +9,9 @@
  *   coef        : real(8)(1:norder, 1:norder), coef(j, n) for reduced order n
  *
  * The mixed-precision arithmetic follows Fortran's promotion rules exactly:
- * `mysum = mysum + coef(k,n)*(u(a) - u(b))` is a float difference, promoted to
- * double, multiplied by the double coefficient, added to the promoted float
- * accumulator and rounded back to float.
+ * `mysum = mysum + coef(k,n)*(u(a) - u(b))` is a real_t difference, promoted to
+ * double, multiplied by the double coefficient, added to the promoted real_t
+ * accumulator and rounded back to real_t.
  *
  * Every routine is exported twice: with a trailing underscore and all
  * arguments by reference (the gfortran ABI the shipped libHybrid.so/libPML.so
@@ -43,9 +43,9 @@ static grid_t mkgrid(int nx, int nz, int npml, int izt)
     return g;
 }
 
-static inline float acc(float s, double c, float d)
+static inline real_t acc(real_t s, double c, real_t d)
 {
-    return (float)((double)s + c * (double)d);
+    return (real_t)((double)s + c * (double)d);
 }
 
 /* ---------------------------------------------------------------------- */
@@ -95,24 +95,24 @@ void fdfk_op_fd_coef1(int norder, double *coef) { fd_coef_collocated(norder, coe
 void fdfk_op_fd_coef2(int norder, double *coef) { fd_coef_collocated(norder, coef, 1); }
 
 /* ---------------------------------------------------------------------- */
-/* check_stability: src/Submain.f90:118-164.  Returns dt_stable (float).  */
+/* check_stability: src/Submain.f90:118-164.  Returns dt_stable (real_t).  */
 /* ---------------------------------------------------------------------- */
-float fdfk_op_dt_stable(int nx, int nz, int npml, int izt, int norder, float dx, float dz,
-                        const double *coef2, const float *c)
+real_t fdfk_op_dt_stable(int nx, int nz, int npml, int izt, int norder, real_t dx, real_t dz,
+                        const double *coef2, const real_t *c)
 {
-    float h = dx > dz ? dx : dz;
-    float cx = (h / dx) * (h / dx);
-    float cz = (h / dz) * (h / dz);
+    real_t h = dx > dz ? dx : dz;
+    real_t cx = (h / dx) * (h / dx);
+    real_t cz = (h / dz) * (h / dz);
     double sa = 0.0, s = 0.0;
     for (int j = 1; j <= norder; ++j) {
         sa += fabs(COEF(coef2, j, norder));
         s += COEF(coef2, j, norder);
     }
-    float cfl = sqrtf((float)(2.0 / ((double)(cx + cz) * (sa + s))));
+    real_t cfl = REAL_SQRT((real_t)(2.0 / ((double)(cx + cz) * (sa + s))));
     size_t ncell = (size_t)(nz + npml - izt + 1) * (size_t)(nx + 2 * npml);
-    float vpmax = 0.0f;
+    real_t vpmax = 0.0f;
     for (size_t i = 0; i < ncell; ++i) {
-        float v = sqrtf((c[3 * i + 1] + 2.0f * c[3 * i + 2]) / c[3 * i + 0]);
+        real_t v = REAL_SQRT((c[3 * i + 1] + 2.0f * c[3 * i + 2]) / c[3 * i + 0]);
         if (v > vpmax) vpmax = v;
     }
     return cfl * h / vpmax;
@@ -121,26 +121,26 @@ float fdfk_op_dt_stable(int nx, int nz, int npml, int izt, int norder, float dx,
 /* ---------------------------------------------------------------------- */
 /* diff1: src/Submain.f90:167-212 (pointwise collocated 1st derivative)   */
 /* ---------------------------------------------------------------------- */
-float fdfk_op_diff1(int norder, int dire, int nx, int nz, int npml, int izt, int ix, int iz,
-                    float d, const double *coef, const float *u)
+real_t fdfk_op_diff1(int norder, int dire, int nx, int nz, int npml, int izt, int ix, int iz,
+                    real_t d, const double *coef, const real_t *u)
 {
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
     int nox = IMIN(IMIN(ix + npml - 1, nx + npml - ix), norder);
     int noz = IMIN(IMIN(iz - izt, nz + npml - iz), norder);
     int kx = 2 - dire, kz = dire - 1;
     int node = kx * nox + kz * noz;
-    float s = 0.0f;
+    real_t s = 0.0f;
     for (int k = 1; k <= node; ++k)
         s = acc(s, COEF(coef, k, node), G(u, iz + kz * k, ix + kx * k) - G(u, iz - kz * k, ix - kx * k));
     return s / d;
 }
 
 /* diffx1: src/Submain.f90:215-249 (1st derivative along a 1-D row). */
-float fdfk_op_diffx1(int norder, int nx, int npml, int ix, float dx, const double *coef, const float *u)
+real_t fdfk_op_diffx1(int norder, int nx, int npml, int ix, real_t dx, const double *coef, const real_t *u)
 {
     int no = IMIN(IMIN(ix + npml - 1, nx + npml - ix), norder);
-    const float *r = u - (1 - npml); /* r[i] == u(i) */
-    float s = 0.0f;
+    const real_t *r = u - (1 - npml); /* r[i] == u(i) */
+    real_t s = 0.0f;
     for (int k = 1; k <= no; ++k) s = acc(s, COEF(coef, k, no), r[ix + k] - r[ix - k]);
     return s / dx;
 }
@@ -150,27 +150,27 @@ float fdfk_op_diffx1(int norder, int nx, int npml, int ix, float dx, const doubl
 /* ---------------------------------------------------------------------- */
 
 /* diffzx_reg: src/Submain.f90:251-409, active part 352-406. */
-void fdfk_op_diffzx_reg(int norder, int nx, int nz, int npml, int izt, float dx, float dz,
-                        const double *coef, const float *mat, const float *u, float *out)
+void fdfk_op_diffzx_reg(int norder, int nx, int nz, int npml, int izt, real_t dx, real_t dz,
+                        const double *coef, const real_t *mat, const real_t *u, real_t *out)
 {
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
     size_t n = (size_t)g->ldz * g->ldx;
-    float *v = (float *)calloc(n, sizeof(float));
+    real_t *v = (real_t *)calloc(n, sizeof(real_t));
 #pragma omp parallel for schedule(static)
     for (int iz = 2; iz <= nz; ++iz) {
         int no = IMIN(IMIN(iz - izt, nz + npml - iz), norder);
         for (int ix = 1 - norder; ix <= nx + norder; ++ix) {
-            float s = 0.0f;
+            real_t s = 0.0f;
             for (int k = 1; k <= no; ++k) s = acc(s, COEF(coef, k, no), G(u, iz + k, ix) - G(u, iz - k, ix));
             G(v, iz, ix) = G(mat, iz, ix) * s / dz;
         }
     }
-    memset(out, 0, n * sizeof(float));
+    memset(out, 0, n * sizeof(real_t));
 #pragma omp parallel for schedule(static)
     for (int ix = 1; ix <= nx; ++ix) {
         int no = IMIN(IMIN(ix + npml - 1, nx + npml - ix), norder);
         for (int iz = 2; iz <= nz; ++iz) {
-            float s = 0.0f;
+            real_t s = 0.0f;
             for (int k = 1; k <= no; ++k) s = acc(s, COEF(coef, k, no), G(v, iz, ix + k) - G(v, iz, ix - k));
             G(out, iz, ix) = s / dx;
         }
@@ -187,31 +187,31 @@ static inline int in_rect(int iz, int ix, int z_lo, int z_hi, int x_lo, int x_hi
 }
 
 /* diffzx_pml: src/Submain.f90:411-507. */
-void fdfk_op_diffzx_pml(int norder, int nx, int nz, int npml, int izt, float dx, float dz,
-                        const double *coef, const float *mat, const float *u, float *out)
+void fdfk_op_diffzx_pml(int norder, int nx, int nz, int npml, int izt, real_t dx, real_t dz,
+                        const double *coef, const real_t *mat, const real_t *u, real_t *out)
 {
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
     size_t n = (size_t)g->ldz * g->ldx;
-    float *v = (float *)calloc(n, sizeof(float));
+    real_t *v = (real_t *)calloc(n, sizeof(real_t));
     /* mask = 1; mask(1:nz, norder+1:nx-norder) = 0; mask(izt,:) = 0 */
 #pragma omp parallel for schedule(static)
     for (int iz = izt + 1; iz <= nz + npml - 1; ++iz) {
         int no = IMIN(IMIN(iz - izt, nz + npml - iz), norder);
         for (int ix = 2 - npml; ix <= nx + npml - 1; ++ix) {
             if (in_rect(iz, ix, 1, nz, norder + 1, nx - norder)) continue;
-            float s = 0.0f;
+            real_t s = 0.0f;
             for (int k = 1; k <= no; ++k) s = acc(s, COEF(coef, k, no), G(u, iz + k, ix) - G(u, iz - k, ix));
             G(v, iz, ix) = G(mat, iz, ix) * s / dz;
         }
     }
-    memset(out, 0, n * sizeof(float));
+    memset(out, 0, n * sizeof(real_t));
     /* mask = 1; mask(1:nz, 1:nx) = 0; mask(izt,:) = 0 */
 #pragma omp parallel for schedule(static)
     for (int ix = 2 - npml; ix <= nx + npml - 1; ++ix) {
         int no = IMIN(IMIN(ix + npml - 1, nx + npml - ix), norder);
         for (int iz = izt + 1; iz <= nz + npml - 1; ++iz) {
             if (in_rect(iz, ix, 1, nz, 1, nx)) continue;
-            float s = 0.0f;
+            real_t s = 0.0f;
             for (int k = 1; k <= no; ++k) s = acc(s, COEF(coef, k, no), G(v, iz, ix + k) - G(v, iz, ix - k));
             G(out, iz, ix) = s / dx;
         }
@@ -220,27 +220,27 @@ void fdfk_op_diffzx_pml(int norder, int nx, int nz, int npml, int izt, float dx,
 }
 
 /* diffxz_reg: src/Submain.f90:509-664, active part 608-661. */
-void fdfk_op_diffxz_reg(int norder, int nx, int nz, int npml, int izt, float dx, float dz,
-                        const double *coef, const float *mat, const float *u, float *out)
+void fdfk_op_diffxz_reg(int norder, int nx, int nz, int npml, int izt, real_t dx, real_t dz,
+                        const double *coef, const real_t *mat, const real_t *u, real_t *out)
 {
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
     size_t n = (size_t)g->ldz * g->ldx;
-    float *v = (float *)calloc(n, sizeof(float));
+    real_t *v = (real_t *)calloc(n, sizeof(real_t));
 #pragma omp parallel for schedule(static)
     for (int ix = 1; ix <= nx; ++ix) {
         int no = IMIN(IMIN(ix + npml - 1, nx + npml - ix), norder);
         for (int iz = 1; iz <= nz + norder; ++iz) {
-            float s = 0.0f;
+            real_t s = 0.0f;
             for (int k = 1; k <= no; ++k) s = acc(s, COEF(coef, k, no), G(u, iz, ix + k) - G(u, iz, ix - k));
             G(v, iz, ix) = G(mat, iz, ix) * s / dx;
         }
     }
-    memset(out, 0, n * sizeof(float));
+    memset(out, 0, n * sizeof(real_t));
 #pragma omp parallel for schedule(static)
     for (int iz = 2; iz <= nz; ++iz) {
         int no = IMIN(IMIN(iz - izt, nz + npml - iz), norder);
         for (int ix = 1; ix <= nx; ++ix) {
-            float s = 0.0f;
+            real_t s = 0.0f;
             for (int k = 1; k <= no; ++k) s = acc(s, COEF(coef, k, no), G(v, iz + k, ix) - G(v, iz - k, ix));
             G(out, iz, ix) = s / dz;
         }
@@ -249,31 +249,31 @@ void fdfk_op_diffxz_reg(int norder, int nx, int nz, int npml, int izt, float dx,
 }
 
 /* diffxz_pml: src/Submain.f90:666-762. */
-void fdfk_op_diffxz_pml(int norder, int nx, int nz, int npml, int izt, float dx, float dz,
-                        const double *coef, const float *mat, const float *u, float *out)
+void fdfk_op_diffxz_pml(int norder, int nx, int nz, int npml, int izt, real_t dx, real_t dz,
+                        const double *coef, const real_t *mat, const real_t *u, real_t *out)
 {
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
     size_t n = (size_t)g->ldz * g->ldx;
-    float *v = (float *)calloc(n, sizeof(float));
+    real_t *v = (real_t *)calloc(n, sizeof(real_t));
     /* mask = 1; mask(1:nz-norder, 1:nx) = 0 */
 #pragma omp parallel for schedule(static)
     for (int ix = 2 - npml; ix <= nx + npml - 1; ++ix) {
         int no = IMIN(IMIN(ix + npml - 1, nx + npml - ix), norder);
         for (int iz = izt; iz <= nz + npml - 1; ++iz) {
             if (in_rect(iz, ix, 1, nz - norder, 1, nx)) continue;
-            float s = 0.0f;
+            real_t s = 0.0f;
             for (int k = 1; k <= no; ++k) s = acc(s, COEF(coef, k, no), G(u, iz, ix + k) - G(u, iz, ix - k));
             G(v, iz, ix) = G(mat, iz, ix) * s / dx;
         }
     }
-    memset(out, 0, n * sizeof(float));
+    memset(out, 0, n * sizeof(real_t));
     /* mask = 1; mask(1:nz, 1:nx) = 0; mask(izt,:) = 0 */
 #pragma omp parallel for schedule(static)
     for (int iz = izt + 1; iz <= nz + npml - 1; ++iz) {
         int no = IMIN(IMIN(iz - izt, nz + npml - iz), norder);
         for (int ix = 2 - npml; ix <= nx + npml - 1; ++ix) {
             if (in_rect(iz, ix, 1, nz, 1, nx)) continue;
-            float s = 0.0f;
+            real_t s = 0.0f;
             for (int k = 1; k <= no; ++k) s = acc(s, COEF(coef, k, no), G(v, iz + k, ix) - G(v, iz - k, ix));
             G(out, iz, ix) = s / dz;
         }
@@ -286,69 +286,69 @@ void fdfk_op_diffxz_pml(int norder, int nx, int nz, int npml, int izt, float dx,
 /* ---------------------------------------------------------------------- */
 
 /* One point of d/dx(M d/dx u): src/Submain.f90:814-837. */
-static inline float x2_point(const grid_t *g, int norder, const double *coef, const float *mat,
-                             const float *u, int iz, int ix)
+static inline real_t x2_point(const grid_t *g, int norder, const double *coef, const real_t *mat,
+                             const real_t *u, int iz, int ix)
 {
     int nx = g->nx, npml = g->npml;
     int no = IMIN(IMIN(ix + npml - 1, nx + npml - ix), norder);
-    float s = 0.0f;
+    real_t s = 0.0f;
     for (int k = 1; k <= no; ++k) {
         int i = k - 1; /* int((2*k-1)/2) */
         int n1 = IMIN(IMIN(ix + i + npml - 1, nx + npml - ix - i), norder);
-        float s1 = 0.0f;
+        real_t s1 = 0.0f;
         for (int j = 1; j <= n1; ++j) s1 = acc(s1, COEF(coef, j, n1), G(u, iz, ix + j + k - 1) - G(u, iz, ix - j + k));
         int n2 = IMIN(IMIN(ix - i + npml - 1, nx + npml - ix + i), norder);
-        float s2 = 0.0f;
+        real_t s2 = 0.0f;
         for (int j = 1; j <= n2; ++j) s2 = acc(s2, COEF(coef, j, n2), G(u, iz, ix + j - k) - G(u, iz, ix - j - k + 1));
-        float hp = 2.0f / (1.0f / G(mat, iz, ix + k) + 1.0f / G(mat, iz, ix + k - 1));
-        float hm = 2.0f / (1.0f / G(mat, iz, ix - k + 1) + 1.0f / G(mat, iz, ix - k));
+        real_t hp = 2.0f / (1.0f / G(mat, iz, ix + k) + 1.0f / G(mat, iz, ix + k - 1));
+        real_t hm = 2.0f / (1.0f / G(mat, iz, ix - k + 1) + 1.0f / G(mat, iz, ix - k));
         s = acc(s, COEF(coef, k, no), hp * s1 - hm * s2);
     }
     return s;
 }
 
 /* One point of d/dz(M d/dz u): src/Submain.f90:988-1011. */
-static inline float z2_point(const grid_t *g, int norder, const double *coef, const float *mat,
-                             const float *u, int iz, int ix)
+static inline real_t z2_point(const grid_t *g, int norder, const double *coef, const real_t *mat,
+                             const real_t *u, int iz, int ix)
 {
     int nz = g->nz, npml = g->npml, izt = g->izt;
     int no = IMIN(IMIN(iz - izt, nz + npml - iz), norder);
-    float s = 0.0f;
+    real_t s = 0.0f;
     for (int k = 1; k <= no; ++k) {
         int i = k - 1;
         int n1 = IMIN(IMIN(iz + i - izt, nz + npml - iz - i), norder);
-        float s1 = 0.0f;
+        real_t s1 = 0.0f;
         for (int j = 1; j <= n1; ++j) s1 = acc(s1, COEF(coef, j, n1), G(u, iz + j + k - 1, ix) - G(u, iz - j + k, ix));
         int n2 = IMIN(IMIN(iz - i - izt, nz + npml - iz + i), norder);
-        float s2 = 0.0f;
+        real_t s2 = 0.0f;
         for (int j = 1; j <= n2; ++j) s2 = acc(s2, COEF(coef, j, n2), G(u, iz + j - k, ix) - G(u, iz - j - k + 1, ix));
-        float hp = 2.0f / (1.0f / G(mat, iz + k, ix) + 1.0f / G(mat, iz + k - 1, ix));
-        float hm = 2.0f / (1.0f / G(mat, iz - k + 1, ix) + 1.0f / G(mat, iz - k, ix));
+        real_t hp = 2.0f / (1.0f / G(mat, iz + k, ix) + 1.0f / G(mat, iz + k - 1, ix));
+        real_t hm = 2.0f / (1.0f / G(mat, iz - k + 1, ix) + 1.0f / G(mat, iz - k, ix));
         s = acc(s, COEF(coef, k, no), hp * s1 - hm * s2);
     }
     return s;
 }
 
-/* diffx2_reg: src/Submain.f90:764-849.  dx2 = 1.d0/(dx*dx) stored as float. */
-void fdfk_op_diffx2_reg(int norder, int nx, int nz, int npml, int izt, float dx,
-                        const double *coef, const float *mat, const float *u, float *out)
+/* diffx2_reg: src/Submain.f90:764-849.  dx2 = 1.d0/(dx*dx) stored as real_t. */
+void fdfk_op_diffx2_reg(int norder, int nx, int nz, int npml, int izt, real_t dx,
+                        const double *coef, const real_t *mat, const real_t *u, real_t *out)
 {
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
-    memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(float));
-    float dx2 = (float)(1.0 / (double)(dx * dx));
+    memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(real_t));
+    real_t dx2 = (real_t)(1.0 / (double)(dx * dx));
     /* mask(1:nz, 1:nx) = 1, loop iz = izt..nz */
 #pragma omp parallel for schedule(static)
     for (int ix = 1; ix <= nx; ++ix)
         for (int iz = IMAX(izt, 1); iz <= nz; ++iz) G(out, iz, ix) = x2_point(g, norder, coef, mat, u, iz, ix) * dx2;
 }
 
-/* diffx2_pml: src/Submain.f90:851-937.  dx2 = 1.0/(dx*dx) in float. */
-void fdfk_op_diffx2_pml(int norder, int nx, int nz, int npml, int izt, float dx,
-                        const double *coef, const float *mat, const float *u, float *out)
+/* diffx2_pml: src/Submain.f90:851-937.  dx2 = 1.0/(dx*dx) in real_t. */
+void fdfk_op_diffx2_pml(int norder, int nx, int nz, int npml, int izt, real_t dx,
+                        const double *coef, const real_t *mat, const real_t *u, real_t *out)
 {
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
-    memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(float));
-    float dx2 = 1.0f / (dx * dx);
+    memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(real_t));
+    real_t dx2 = 1.0f / (dx * dx);
 #pragma omp parallel for schedule(static)
     for (int ix = 2 - npml; ix <= nx + npml - 1; ++ix)
         for (int iz = izt; iz <= nz + npml - 1; ++iz) {
@@ -358,24 +358,24 @@ void fdfk_op_diffx2_pml(int norder, int nx, int nz, int npml, int izt, float dx,
 }
 
 /* diffz2_reg: src/Submain.f90:939-1023. */
-void fdfk_op_diffz2_reg(int norder, int nx, int nz, int npml, int izt, float dz,
-                        const double *coef, const float *mat, const float *u, float *out)
+void fdfk_op_diffz2_reg(int norder, int nx, int nz, int npml, int izt, real_t dz,
+                        const double *coef, const real_t *mat, const real_t *u, real_t *out)
 {
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
-    memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(float));
-    float dz2 = 1.0f / (dz * dz);
+    memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(real_t));
+    real_t dz2 = 1.0f / (dz * dz);
 #pragma omp parallel for schedule(static)
     for (int iz = 2; iz <= nz; ++iz)
         for (int ix = 1; ix <= nx; ++ix) G(out, iz, ix) = z2_point(g, norder, coef, mat, u, iz, ix) * dz2;
 }
 
 /* diffz2_pml: src/Submain.f90:1025-1109. */
-void fdfk_op_diffz2_pml(int norder, int nx, int nz, int npml, int izt, float dz,
-                        const double *coef, const float *mat, const float *u, float *out)
+void fdfk_op_diffz2_pml(int norder, int nx, int nz, int npml, int izt, real_t dz,
+                        const double *coef, const real_t *mat, const real_t *u, real_t *out)
 {
     grid_t gg = mkgrid(nx, nz, npml, izt), *g = &gg;
-    memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(float));
-    float dz2 = 1.0f / (dz * dz);
+    memset(out, 0, (size_t)g->ldz * g->ldx * sizeof(real_t));
+    real_t dz2 = 1.0f / (dz * dz);
 #pragma omp parallel for schedule(static)
     for (int iz = izt + 1; iz <= nz + npml - 1; ++iz)
         for (int ix = 1 - npml; ix <= nx + npml; ++ix) {
@@ -401,22 +401,22 @@ double fdfk_op_delta_weight(double x)
     return 0.0;
 }
 
-void fdfk_op_loadseis(int nx, int nz, int npml, int izt, float x0, float z0, float dx, float dz,
-                      float rx, float rz, const float *ux, const float *uz, float *dispx, float *dispz)
+void fdfk_op_loadseis(int nx, int nz, int npml, int izt, real_t x0, real_t z0, real_t dx, real_t dz,
+                      real_t rx, real_t rz, const real_t *ux, const real_t *uz, real_t *dispx, real_t *dispz)
 {
     int ldz = nz + npml - izt + 1;
-    int irx = (int)floorf((rx - x0) / dx) + 1;
-    int irz = (int)floorf((rz - z0) / dz) + 1;
-    float sx = 0.0f, sz = 0.0f;
+    int irx = (int)floor((rx - x0) / dx) + 1;
+    int irz = (int)floor((rz - z0) / dz) + 1;
+    real_t sx = 0.0f, sz = 0.0f;
     for (int ix = IMAX(1 - npml, irx - 3); ix <= IMIN(nx + npml, irx + 3); ++ix) {
-        double x = fabs((double)((double)(x0 + (float)(ix - 1) * dx) - (double)rx)) / (double)dx;
+        double x = fabs((double)((double)(x0 + (real_t)(ix - 1) * dx) - (double)rx)) / (double)dx;
         double bx = fdfk_op_delta_weight(x);
         for (int iz = IMAX(izt, irz - 3); iz <= IMIN(nz + npml, irz + 3); ++iz) {
-            double z = fabs((double)((double)(z0 + (float)(iz - 1) * dz) - (double)rz)) / (double)dz;
+            double z = fabs((double)((double)(z0 + (real_t)(iz - 1) * dz) - (double)rz)) / (double)dz;
             double ba = bx * fdfk_op_delta_weight(z);
             size_t o = 2 * ((size_t)(iz - izt) + (size_t)(ix - (1 - npml)) * (size_t)ldz);
-            sx = (float)((double)sx + ba * (double)ux[o]);
-            sz = (float)((double)sz + ba * (double)uz[o]);
+            sx = (real_t)((double)sx + ba * (double)ux[o]);
+            sz = (real_t)((double)sz + ba * (double)uz[o]);
         }
     }
     *dispx = sx;
@@ -427,14 +427,14 @@ void fdfk_op_loadseis(int nx, int nz, int npml, int izt, float x0, float z0, flo
 /* gfortran-ABI exports (every argument by reference).                    */
 /* ---------------------------------------------------------------------- */
 void diff1_(const int *norder, const int *dire, const int *nx, const int *nz, const int *npml, const int *izt,
-            const int *ix, const int *iz, const float *d, const double *coef, const float *u, float *tmp)
+            const int *ix, const int *iz, const real_t *d, const double *coef, const real_t *u, real_t *tmp)
 {
     *tmp = fdfk_op_diff1(*norder, *dire, *nx, *nz, *npml, *izt, *ix, *iz, *d, coef, u);
     fdfk_trace_point(1, __builtin_return_address(0), *ix, *iz, *dire, *d, u, *tmp);
 }
 
-void diffx1_(const int *norder, const int *nx, const int *npml, const int *ix, const float *dx,
-             const double *coef, const float *u, float *tmp)
+void diffx1_(const int *norder, const int *nx, const int *npml, const int *ix, const real_t *dx,
+             const double *coef, const real_t *u, real_t *tmp)
 {
     *tmp = fdfk_op_diffx1(*norder, *nx, *npml, *ix, *dx, coef, u);
     fdfk_trace_point(2, __builtin_return_address(0), *ix, 0, 1, *dx, u, *tmp);
@@ -442,8 +442,8 @@ void diffx1_(const int *norder, const int *nx, const int *npml, const int *ix, c
 
 #define MIXED_EXPORT(name)                                                                              \
     void name##_(const int *norder, const int *nx, const int *nz, const int *npml, const int *izt,      \
-                 const float *dx, const float *dz, const double *coef, const float *mat, const float *u, \
-                 float *out)                                                                            \
+                 const real_t *dx, const real_t *dz, const double *coef, const real_t *mat, const real_t *u, \
+                 real_t *out)                                                                            \
     {                                                                                                   \
         fdfk_trace_hook(#name, *norder, *nx, *nz, *npml, *izt, mat, u, out);                            \
         fdfk_op_##name(*norder, *nx, *nz, *npml, *izt, *dx, *dz, coef, mat, u, out);                    \
@@ -451,7 +451,7 @@ void diffx1_(const int *norder, const int *nx, const int *npml, const int *ix, c
     }
 #define SECOND_EXPORT(name)                                                                             \
     void name##_(const int *norder, const int *nx, const int *nz, const int *npml, const int *izt,      \
-                 const float *d, const double *coef, const float *mat, const float *u, float *out)      \
+                 const real_t *d, const double *coef, const real_t *mat, const real_t *u, real_t *out)      \
     {                                                                                                   \
         fdfk_trace_hook(#name, *norder, *nx, *nz, *npml, *izt, mat, u, out);                            \
         fdfk_op_##name(*norder, *nx, *nz, *npml, *izt, *d, coef, mat, u, out);                          \
@@ -461,16 +461,16 @@ void diffx1_(const int *norder, const int *nx, const int *npml, const int *ix, c
 /* Optional observation hooks: the reference harness overrides these to record
  * which operators the shipped libraries call; the defaults do nothing. */
 __attribute__((weak)) void fdfk_trace_hook(const char *name, int norder, int nx, int nz, int npml, int izt,
-                                           const float *mat, const float *u, float *out)
+                                           const real_t *mat, const real_t *u, real_t *out)
 {
     (void)name; (void)norder; (void)nx; (void)nz; (void)npml; (void)izt; (void)mat; (void)u; (void)out;
 }
-__attribute__((weak)) void fdfk_trace_point(int which, const void *caller, int ix, int iz, int dire, float d,
-                                            const float *u, float val)
+__attribute__((weak)) void fdfk_trace_point(int which, const void *caller, int ix, int iz, int dire, real_t d,
+                                            const real_t *u, real_t val)
 {
     (void)which; (void)caller; (void)ix; (void)iz; (void)dire; (void)d; (void)u; (void)val;
 }
-__attribute__((weak)) void fdfk_trace_post(const char *name, int nx, int nz, int npml, int izt, float *out)
+__attribute__((weak)) void fdfk_trace_post(const char *name, int nx, int nz, int npml, int izt, real_t *out)
 {
     (void)name; (void)nx; (void)nz; (void)npml; (void)izt; (void)out;
 }

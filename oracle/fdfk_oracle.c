@@ -12,7 +12,7 @@
  *      u^{n+1} = 2 u^n - u^{n-1} + dt^2/rho * F,  level 2 <- old level 1.
  *    F_x = dxx(l2m ux) + dzx(lam uz) + dzz(mu ux) + dxz(mu uz)
  *    F_z = dzz(l2m uz) + dxz(lam ux) + dxx(mu uz) + dzx(mu ux)
- *    with the *_reg operators (l2m = lam + 2 mu computed in float).
+ *    with the *_reg operators (l2m = lam + 2 mu computed in real_t).
  * 2. Hybrid injection (Alterman-Karal): the interior operators act on
  *    u + u_b(it) where u_b is added on the outer strips (Omega_II: the *_pml
  *    background strips); the PML operators act on u - u_b(it) where u_b is
@@ -66,7 +66,7 @@ static inline size_t si(int n1, int n2, int r, int c, int t)
     return (size_t)r + (size_t)n1 * ((size_t)c + (size_t)n2 * (size_t)t);
 }
 
-static double dx1_row(const geo_t *g, const double *coef1, const float *row_base, size_t stride, int ix, float dx)
+static double dx1_row(const geo_t *g, const double *coef1, const real_t *row_base, size_t stride, int ix, real_t dx)
 {
     /* collocated x-derivative of a grid row (row_base = element (iz, 1-npml), stride = ldz) */
     int norder = g->norder;
@@ -78,7 +78,7 @@ static double dx1_row(const geo_t *g, const double *coef1, const float *row_base
     return s / dx;
 }
 
-static double dx1_rowd(const geo_t *g, const double *coef1, const double *row, int ix, float dx)
+static double dx1_rowd(const geo_t *g, const double *coef1, const double *row, int ix, real_t dx)
 {
     int norder = g->norder;
     int no = IMIN(IMIN(ix + g->npml - 1, g->nx + g->npml - ix), norder);
@@ -89,7 +89,7 @@ static double dx1_rowd(const geo_t *g, const double *coef1, const double *row, i
 }
 
 /* pointwise collocated derivative in x (dire 1) or z (dire 2) of a double field */
-static double cd1(const geo_t *g, const double *coef1, const double *u, int iz, int ix, int dire, float d)
+static double cd1(const geo_t *g, const double *coef1, const double *u, int iz, int ix, int dire, real_t d)
 {
     int norder = g->norder;
     double s = 0.0;
@@ -105,11 +105,11 @@ static double cd1(const geo_t *g, const double *coef1, const double *u, int iz, 
 
 enum { OP_X2_L2M_X, OP_Z2_L2M_Z, OP_ZX_LAM_Z, OP_XZ_LAM_X, OP_Z2_MU_X, OP_X2_MU_Z, OP_XZ_MU_Z, OP_ZX_MU_X, NOPS };
 
-static void run_ops(const fdfk_oracle_params *p, int pml, const float *l2m, const float *lam, const float *mu,
-                    const double *coef0, const double *coef1, const float *tx, const float *tz, float *const out[NOPS])
+static void run_ops(const fdfk_oracle_params *p, int pml, const real_t *l2m, const real_t *lam, const real_t *mu,
+                    const double *coef0, const double *coef1, const real_t *tx, const real_t *tz, real_t *const out[NOPS])
 {
     int a0 = p->norder, nx = p->nx, nz = p->nz, npml = p->npml, izt = p->izt;
-    float dx = p->dx, dz = p->dz;
+    real_t dx = p->dx, dz = p->dz;
     if (!pml) {
         fdfk_op_diffx2_reg(a0, nx, nz, npml, izt, dx, coef0, l2m, tx, out[OP_X2_L2M_X]);
         fdfk_op_diffz2_reg(a0, nx, nz, npml, izt, dz, coef0, l2m, tz, out[OP_Z2_L2M_Z]);
@@ -132,12 +132,12 @@ static void run_ops(const fdfk_oracle_params *p, int pml, const float *l2m, cons
 }
 
 /* Add (sign +1) the outer background strips or remove (sign -1) the inner ones. */
-static void apply_strips(const fdfk_oracle_params *p, const geo_t *g, int it, const float *const strips[12], int comp,
-                         int outer, float *t)
+static void apply_strips(const fdfk_oracle_params *p, const geo_t *g, int it, const real_t *const strips[12], int comp,
+                         int outer, real_t *t)
 {
     int nx = p->nx, nz = p->nz, nbd = p->nbd;
     if (outer) {
-        const float *L = strips[6 + comp], *Rr = strips[8 + comp], *B = strips[10 + comp];
+        const real_t *L = strips[6 + comp], *Rr = strips[8 + comp], *B = strips[10 + comp];
         for (int c = 0; c < nbd; ++c)
             for (int r = 0; r < nz; ++r) {
                 t[gi(g, 1 + r, 1 - nbd + c)] += L[si(nz, nbd, r, c, it)];
@@ -146,7 +146,7 @@ static void apply_strips(const fdfk_oracle_params *p, const geo_t *g, int it, co
         for (int c = 0; c < nx + 2 * nbd; ++c)
             for (int r = 0; r < nbd; ++r) t[gi(g, nz + 1 + r, 1 - nbd + c)] += B[si(nbd, nx + 2 * nbd, r, c, it)];
     } else {
-        const float *L = strips[0 + comp], *Rr = strips[2 + comp], *B = strips[4 + comp];
+        const real_t *L = strips[0 + comp], *Rr = strips[2 + comp], *B = strips[4 + comp];
         for (int c = 0; c < nbd; ++c)
             for (int r = 0; r < nz - nbd; ++r) {
                 t[gi(g, 1 + r, 1 + c)] -= L[si(nz - nbd, nbd, r, c, it)];
@@ -159,26 +159,26 @@ static void apply_strips(const fdfk_oracle_params *p, const geo_t *g, int it, co
 
 static inline double hmean(double a, double b) { return 2.0 / (1.0 / a + 1.0 / b); }
 
-int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const float *const strips[12], const float *c,
-                            const double *coef0, const double *coef1, float *ux, float *uz, float *const bp[12],
-                            float *const bu[24])
+int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const real_t *const strips[12], const real_t *c,
+                            const double *coef0, const double *coef1, real_t *ux, real_t *uz, real_t *const bp[12],
+                            real_t *const bu[24])
 {
     if (p->izt != 1) return -2;
     if (p->norder < 1 || p->nbd != 2 * p->norder - 1 || p->npml < p->nbd || p->nz <= p->nbd || p->nx < 1) return -1;
     geo_t G = {p->nx, p->nz, p->npml, p->izt, p->nz + p->npml - p->izt + 1, p->nx + 2 * p->npml, p->norder, p->nbd};
     const geo_t *g = &G;
     int nx = p->nx, nz = p->nz, npml = p->npml;
-    float dx = p->dx, dz = p->dz;
+    real_t dx = p->dx, dz = p->dz;
     double dt = p->dt;
     size_t n = (size_t)g->ldz * g->ldx;
 
-    float *w = (float *)malloc(sizeof(float) * n * (6 + 2 * NOPS));
+    real_t *w = (real_t *)malloc(sizeof(real_t) * n * (6 + 2 * NOPS));
     double *wd = (double *)malloc(sizeof(double) * n * 2);
     if (!w || !wd) { free(w); free(wd); return -3; }
-    float *rho = w, *lam = w + n, *mu = w + 2 * n, *l2m = w + 3 * n, *tx = w + 4 * n, *tz = w + 5 * n;
-    float *ops[NOPS];
+    real_t *rho = w, *lam = w + n, *mu = w + 2 * n, *l2m = w + 3 * n, *tx = w + 4 * n, *tz = w + 5 * n;
+    real_t *ops[NOPS];
     for (int k = 0; k < NOPS; ++k) ops[k] = w + (6 + k) * n;
-    float *pops[NOPS];
+    real_t *pops[NOPS];
     for (int k = 0; k < NOPS; ++k) pops[k] = w + (6 + NOPS + k) * n;
     for (size_t i = 0; i < n; ++i) {
         rho[i] = c[3 * i]; lam[i] = c[3 * i + 1]; mu[i] = c[3 * i + 2];
@@ -192,7 +192,7 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const float *co
     run_ops(p, 0, l2m, lam, mu, coef0, coef1, tx, tz, ops);
 
     /* -------- PML: operators on u^n - u_b(inner strips) (reads only level 1) -------- */
-    float *px = (float *)malloc(sizeof(float) * n), *pz = (float *)malloc(sizeof(float) * n);
+    real_t *px = (real_t *)malloc(sizeof(real_t) * n), *pz = (real_t *)malloc(sizeof(real_t) * n);
     if (!px || !pz) { free(w); free(wd); free(px); free(pz); return -3; }
     for (size_t i = 0; i < n; ++i) { px[i] = ux[2 * i]; pz[i] = uz[2 * i]; }
     apply_strips(p, g, it, strips, 0, 0, px);
@@ -202,7 +202,7 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const float *co
     for (size_t i = 0; i < n; ++i) { Sx[i] = px[i]; Sz[i] = pz[i]; }
 
     /* -------- interior update (rows 1..nz, cols 1..nx) -------- */
-    float *nux1 = (float *)malloc(sizeof(float) * n), *nuz1 = (float *)malloc(sizeof(float) * n);
+    real_t *nux1 = (real_t *)malloc(sizeof(real_t) * n), *nuz1 = (real_t *)malloc(sizeof(real_t) * n);
     if (!nux1 || !nuz1) { free(w); free(wd); free(px); free(pz); free(nux1); free(nuz1); return -3; }
 #pragma omp parallel for schedule(static)
     for (int ix = 1; ix <= nx; ++ix) {
@@ -244,8 +244,8 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const float *co
                 Fz = (double)ops[OP_Z2_L2M_Z][i] + (double)ops[OP_XZ_LAM_X][i] + (double)ops[OP_X2_MU_Z][i] +
                      (double)ops[OP_ZX_MU_X][i];
             }
-            nux1[i] = (float)(2.0 * ux[2 * i] - (double)ux[2 * i + 1] + dt * dt * Fx / (double)rho[i]);
-            nuz1[i] = (float)(2.0 * uz[2 * i] - (double)uz[2 * i + 1] + dt * dt * Fz / (double)rho[i]);
+            nux1[i] = (real_t)(2.0 * ux[2 * i] - (double)ux[2 * i + 1] + dt * dt * Fx / (double)rho[i]);
+            nuz1[i] = (real_t)(2.0 * uz[2 * i] - (double)uz[2 * i + 1] + dt * dt * Fz / (double)rho[i]);
         }
     }
 
@@ -329,10 +329,10 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const float *co
                         S1 = (double)mu[i] * cd1(g, coef1, Sz, iz, ix, 1, dx);
                         if (side == 2) S3 = (double)l2m[i] * cd1(g, coef1, Sz, iz, ix, 2, dz);
                     }
-                    float *bpx = bp[side == 0 ? 0 + comp : side == 1 ? 2 + comp : 8 + 2 * comp];
-                    float *bpz = side == 2 ? bp[9 + 2 * comp] : NULL;
+                    real_t *bpx = bp[side == 0 ? 0 + comp : side == 1 ? 2 + comp : 8 + 2 * comp];
+                    real_t *bpz = side == 2 ? bp[9 + 2 * comp] : NULL;
                     int base = (side == 0 ? 0 : side == 1 ? 6 : 12) + 3 * comp;
-                    float *b1 = bu[base], *b2 = bu[base + 1], *b3 = bu[base + 2];
+                    real_t *b1 = bu[base], *b2 = bu[base + 1], *b3 = bu[base + 2];
                     double Px = bpx[ap];
                     double Pxn = ((1.0 - yx / 2) * Px - dt * dxp * S1) / (1.0 + yx / 2);
                     double u1 = b1[ab], u1m = b1[ab + 1];
@@ -348,17 +348,17 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const float *co
                     if (bpz) {
                         double Pz = bpz[ap];
                         double Pzn = ((1.0 - yz / 2) * Pz - dt * dzp * S3) / (1.0 + yz / 2);
-                        bpz[ap] = (float)Pzn;
+                        bpz[ap] = (real_t)Pzn;
                         n3 = ((2.0 - yz * yz) * u3 - (1.0 - yz) * u3m + k * (F3 + (Pzn + Pz) / 2.0)) / (1.0 + yz);
                     } else {
                         n3 = 2.0 * u3 - u3m + k * F3;
                     }
-                    bpx[ap] = (float)Pxn;
-                    b1[ab + 1] = b1[ab]; b1[ab] = (float)n1;
-                    b2[ab + 1] = b2[ab]; b2[ab] = (float)n2;
-                    b3[ab + 1] = b3[ab]; b3[ab] = (float)n3;
-                    if (comp == 0) nux1[i] = (float)(n1 + n2 + n3);
-                    else nuz1[i] = (float)(n1 + n2 + n3);
+                    bpx[ap] = (real_t)Pxn;
+                    b1[ab + 1] = b1[ab]; b1[ab] = (real_t)n1;
+                    b2[ab + 1] = b2[ab]; b2[ab] = (real_t)n2;
+                    b3[ab + 1] = b3[ab]; b3[ab] = (real_t)n3;
+                    if (comp == 0) nux1[i] = (real_t)(n1 + n2 + n3);
+                    else nuz1[i] = (real_t)(n1 + n2 + n3);
                 }
             }
         }
@@ -377,17 +377,17 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const float *co
     return 0;
 }
 
-int fdfk_oracle_simulate(const fdfk_oracle_params *p, const float *const strips[12], const float *c, int nrcv,
-                         const float *rx, const float *rz, float x0, float z0, int nstp, int nsis,
-                         float *seisx, float *seisz, int steps_limit)
+int fdfk_oracle_simulate(const fdfk_oracle_params *p, const real_t *const strips[12], const real_t *c, int nrcv,
+                         const real_t *rx, const real_t *rz, real_t x0, real_t z0, int nstp, int nsis,
+                         real_t *seisx, real_t *seisz, int steps_limit)
 {
     if (p->izt != 1) return -2;
     int nx = p->nx, nz = p->nz, npml = p->npml, norder = p->norder;
     size_t n = (size_t)(nz + npml) * (size_t)(nx + 2 * npml);
-    float *ux = (float *)calloc(2 * n, sizeof(float)), *uz = (float *)calloc(2 * n, sizeof(float));
+    real_t *ux = (real_t *)calloc(2 * n, sizeof(real_t)), *uz = (real_t *)calloc(2 * n, sizeof(real_t));
     size_t side = (size_t)nz * npml, tb = (size_t)npml * (nx + 2 * npml);
-    float *bpbuf = (float *)calloc(4 * side + 8 * tb, sizeof(float));
-    float *bubuf = (float *)calloc(2 * (12 * side + 12 * tb), sizeof(float));
+    real_t *bpbuf = (real_t *)calloc(4 * side + 8 * tb, sizeof(real_t));
+    real_t *bubuf = (real_t *)calloc(2 * (12 * side + 12 * tb), sizeof(real_t));
     double *coef0 = (double *)malloc(sizeof(double) * norder * norder), *coef1 = (double *)malloc(sizeof(double) * norder * norder);
     if (!ux || !uz || !bpbuf || !bubuf || !coef0 || !coef1) {
         free(ux); free(uz); free(bpbuf); free(bubuf); free(coef0); free(coef1);
@@ -395,9 +395,9 @@ int fdfk_oracle_simulate(const fdfk_oracle_params *p, const float *const strips[
     }
     fdfk_op_fd_coef0(norder, coef0);
     fdfk_op_fd_coef1(norder, coef1);
-    float *bp[12], *bu[24];
+    real_t *bp[12], *bu[24];
     {
-        float *q = bpbuf;
+        real_t *q = bpbuf;
         for (int k = 0; k < 4; ++k) { bp[k] = q; q += side; }
         for (int k = 4; k < 12; ++k) { bp[k] = q; q += tb; }
         q = bubuf;

@@ -174,8 +174,9 @@ def layered_response(model, p, wc, z, incident="P", z_ref=0.0):
     return UR, UZ
 
 
-def background(p, bazs, fk_left, fk_right, x0=0.0, z0=0.0):
-    """Restated comput_background_wavefield: dict of the 12 strips, float32 (n1, n2, nt+1).
+def background(p, bazs, fk_left, fk_right, x0=0.0, z0=0.0, dtype=np.float32):
+    """Restated comput_background_wavefield: dict of the 12 strips (n1, n2, nt+1), float32 as the
+    reference stores them (dtype=np.float64 keeps the FP64 values, for the FP64 oracle).
 
     p: nx, nz, npml, nbd, nt, dt, dx, dz, f0, ds, rayp (s/m), src_type (True = P).
     bazs: back-azimuths (rad) of the nx + 2 npml columns, profile frame.
@@ -210,7 +211,7 @@ def background(p, bazs, fk_left, fk_right, x0=0.0, z0=0.0):
     for name in STRIPS:
         iz, ix = strip_coords(nx, nz, nbd, name)
         side = name[2]
-        arr = np.zeros((len(iz), len(ix), nt + 1), np.float32, order="F")
+        arr = np.zeros((len(iz), len(ix), nt + 1), dtype, order="F")
         for jj, cx in enumerate(ix):
             if side == "b":
                 left = cx <= nbd if cbar >= 0.0 else cx <= nx - nbd
@@ -229,6 +230,6 @@ def background(p, bazs, fk_left, fk_right, x0=0.0, z0=0.0):
             X[:kmax + 1] = W[:kmax + 1, None] * U[:kmax + 1] * ph[:kmax + 1, None]
             X[N - kmax:] = np.conj(X[1:kmax + 1][::-1])
             xt = np.fft.ifft(X, axis=0).real * N
-            arr[:, jj, :] = (xt[:nt + 1].T * np.exp(alpha * tn) / N).astype(np.float32)
+            arr[:, jj, :] = (xt[:nt + 1].T * np.exp(alpha * tn) / N).astype(dtype)
         out[name] = arr
     return out

@@ -8,6 +8,9 @@ use this module.  It loads ``oracle/_build/libfdfk_oracle.so`` (built by
   call (src/FDFK2D.f90:516-522);
 * :func:`simulate` - the restated time loop with receiver sampling
   (src/FDFK2D.f90:465-532);
+* :func:`simulate64` - the same time loop with every field in FP64
+  (``oracle/_build/libfdfk_oracle64.so``): the FP64 oracle the FP32 traces are
+  stated against;
 * :func:`fd_coef0` / :func:`fd_coef1` / :func:`fd_coef2` (src/Submain.f90:1111-1245).
 
 Array conventions match ``oracle/refharness.py``.
@@ -22,6 +25,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libfdfk_oracle.so")
+LIB64 = os.path.join(HERE, "_build", "libfdfk_oracle64.so")
 
 STRIPS = ("uxl_reg", "uzl_reg", "uxr_reg", "uzr_reg", "uxb_reg", "uzb_reg",
           "uxl_pml", "uzl_pml", "uxr_pml", "uzr_pml", "uxb_pml", "uzb_pml")
@@ -52,6 +56,49 @@ def lib():
         _lib.fdfk_oracle_updatedispl.restype = C.c_int
         _lib.fdfk_oracle_simulate.restype = C.c_int
     return _lib
+
+
+class Params64(C.Structure):
+    _fields_ = [("norder", C.c_int), ("nx", C.c_int), ("nz", C.c_int), ("npml", C.c_int), ("izt", C.c_int),
+                ("npower", C.c_int), ("nbd", C.c_int), ("nt", C.c_int), ("dx", C.c_double), ("dz", C.c_double),
+                ("dt", C.c_double), ("vpml", C.c_double), ("R0", C.c_double)]
+
+
+_lib64 = None
+
+
+def lib64():
+    global _lib64
+    if _lib64 is None:
+        if not os.path.exists(LIB64):
+            build()
+        _lib64 = C.CDLL(LIB64)
+        _lib64.fdfk_oracle_simulate.restype = C.c_int
+    return _lib64
+
+
+def simulate64(p, strips, c, rx, rz, x0, z0, nstp, nsis, steps_limit=-1):
+    """The restated time loop in FP64 (inputs widened); returns float64 (seisx, seisz), (nsis+1, nrcv)."""
+    L = lib64()
+    nrcv = len(rx)
+    d = lambda a: np.asfortranarray(a, np.float64)
+    seisx = np.zeros((nsis + 1, nrcv), np.float64, order="F")
+    seisz = np.zeros((nsis + 1, nrcv), np.float64, order="F")
+    st = {k: d(strips[k]) for k in STRIPS}
+    sp = (C.c_void_p * 12)(*[st[k].ctypes.data_as(C.c_void_p) for k in STRIPS])
+    cd = d(c)
+    rxa = np.asarray(rx, np.float64)
+    rza = np.asarray(rz, np.float64)
+    prm = Params64(int(p["norder"]), int(p["nx"]), int(p["nz"]), int(p["npml"]), int(p["izt"]),
+                   int(p.get("npower", 2)), int(p["nbd"]), int(p["nt"]), float(p["dx"]), float(p["dz"]),
+                   float(p["dt"]), float(p["vpml"]), float(p.get("R0", 1e-3)))
+    rc = L.fdfk_oracle_simulate(C.byref(prm), sp, cd.ctypes.data_as(C.c_void_p), C.c_int(nrcv),
+                                rxa.ctypes.data_as(C.c_void_p), rza.ctypes.data_as(C.c_void_p), C.c_double(x0),
+                                C.c_double(z0), C.c_int(nstp), C.c_int(nsis), seisx.ctypes.data_as(C.c_void_p),
+                                seisz.ctypes.data_as(C.c_void_p), C.c_int(steps_limit))
+    if rc != 0:
+        raise RuntimeError(f"FP64 oracle simulate failed: {rc}")
+    return seisx, seisz
 
 
 def params(p: dict) -> Params:
