@@ -28,11 +28,6 @@ struct Ring {
     static constexpr int kWarpFloats = 64 * (kSlotsA * kFieldsA + kSlotsB * kFieldsB);
 };
 
-__device__ __forceinline__ void cp_async8(float* smem, const float* gmem)
-{
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
@@ -40,6 +35,39 @@ __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0
 __device__ __forceinline__ void st_shared2(float* smem, float v0, float v1)
 {
     *reinterpret_cast<float2*>(smem) = make_float2(v0, v1);
+}
+
+// cp.async into a 32-bit shared-space address plus an immediate byte offset.
+template <int OFF>
+__device__ __forceinline__ void cp_async8_s(unsigned s, const float* g)
+{
+    asm volatile("cp.async.ca.shared.global [%0+%2], [%1], 8;\n" ::"r"(s), "l"(g), "n"(OFF) : "memory");
+}
+// z-derivatives of one shuffled column (rows r0-NO .. r0+NO+1), shared by the staggered and
+// the collocated stencils of the same field.
+template <int NO>
+__device__ __forceinline__ void zc_stag(const ZCol<-NO, NO + 1>& z, float& d0, float& d1)
+{
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+    for (int j = 1; j <= NO; ++j) {
+        s0 = fmaf(c_stag[NO][j], z(j) - z(1 - j), s0);
+        s1 = fmaf(c_stag[NO][j], z(j + 1) - z(2 - j), s1);
+    }
+    d0 = s0;
+    d1 = s1;
+}
+template <int NO>
+__device__ __forceinline__ void zc_coll(const ZCol<-NO, NO + 1>& z, float& d0, float& d1)
+{
+    float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+    for (int k = 1; k <= NO; ++k) {
+        s0 = fmaf(c_coll[NO][k], z(k) - z(-k), s0);
+        s1 = fmaf(c_coll[NO][k], z(k + 1) - z(1 - k), s1);
+    }
+    d0 = s0;
+    d1 = s1;
 }
 
 template <int NO, bool EX, bool EZ>
@@ -73,6 +101,11 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
     float* const ringB = ring + 64 * RG::kSlotsA * RG::kFieldsA + 2 * lane;
     auto slotA = [&](int col, int f) -> float* { return ringA + ((col & (RG::kSlotsA - 1)) * RG::kFieldsA + f) * 64; };
     auto slotB = [&](int col, int f) -> float* { return ringB + ((col & (RG::kSlotsB - 1)) * RG::kFieldsB + f) * 64; };
+    // shared-space byte addresses of this lane's pair in field 0 of a column's slot
+    const unsigned sA0 = (unsigned)__cvta_generic_to_shared(ringA), sB0 = (unsigned)__cvta_generic_to_shared(ringB);
+    constexpr int kFA = 64 * 4, kFB = 64 * 4;                       // bytes between fields of a slot
+    auto sA = [&](int col) -> unsigned { return sA0 + (unsigned)((col & (RG::kSlotsA - 1)) * RG::kFieldsA * kFA); };
+    auto sB = [&](int col) -> unsigned { return sB0 + (unsigned)((col & (RG::kSlotsB - 1)) * RG::kFieldsB * kFB); };
     auto rdA = [&](int col, int f) -> float2 { return *reinterpret_cast<const float2*>(slotA(col, f)); };
     auto rdB = [&](int col, int f) -> float2 { return *reinterpret_cast<const float2*>(slotB(col, f)); };
 
@@ -90,10 +123,11 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
             } else {
                 const int o = gofs(col);
                 if (rows_in) {
-                    cp_async8(slotA(col, 0), uxc + o);
-                    cp_async8(slotA(col, 1), uzc + o);
-                    cp_async8(slotA(col, 2), a.lam + o);
-                    cp_async8(slotA(col, 3), a.mu + o);
+                    const unsigned sa = sA(col);
+                    cp_async8_s<0 * kFA>(sa, uxc + o);
+                    cp_async8_s<1 * kFA>(sa, uzc + o);
+                    cp_async8_s<2 * kFA>(sa, a.lam + o);
+                    cp_async8_s<3 * kFA>(sa, a.mu + o);
                 } else {   // a lane straddling the bottom of the grid: rows outside read as u = lambda = 0, mu = 1
                     st_shared2(slotA(col, 0), r0_in ? __ldg(uxc + o) : 0.f, r1_in ? __ldg(uxc + o + 1) : 0.f);
                     st_shared2(slotA(col, 1), r0_in ? __ldg(uzc + o) : 0.f, r1_in ? __ldg(uzc + o + 1) : 0.f);
@@ -105,9 +139,10 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
             if (store && xcol >= xs) {
                 const int oc = gofs(xcol);
                 if (store1) {
-                    cp_async8(slotB(col, 0), a.kdt2 + oc);
-                    cp_async8(slotB(col, 1), uxn + oc);
-                    cp_async8(slotB(col, 2), uzn + oc);
+                    const unsigned sb = sB(col);
+                    cp_async8_s<0 * kFB>(sb, a.kdt2 + oc);
+                    cp_async8_s<1 * kFB>(sb, uxn + oc);
+                    cp_async8_s<2 * kFB>(sb, uzn + oc);
                 } else {
                     st_shared2(slotB(col, 0), __ldg(a.kdt2 + oc), 0.f);
                     st_shared2(slotB(col, 1), uxn[oc], 0.f);
@@ -206,12 +241,13 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
         }
         D2[ND - 1][0] = 0.f; D2[ND - 1][1] = 0.f; D3[ND - 1][0] = 0.f; D3[ND - 1][1] = 0.f;
 
-        // --- z-direction terms of column mc
+        // --- z-direction terms of column mc (one shuffled column per field for every z-stencil)
+        const ZCol<-NO, NO + 1> zz(uz0, uz1), zx(ux0, ux1);
         float z2a0, z2a1, z2b0, z2b1;
         {
             float sza0, sza1, szb0, szb1;
-            dz_stag<NO>(uz0, uz1, sza0, sza1);
-            dz_stag<NO>(ux0, ux1, szb0, szb1);
+            zc_stag<NO>(zz, sza0, sza1);
+            zc_stag<NO>(zx, szb0, szb1);
             const float rl0 = frcp(ln0 + 2.0f * mn0), rl1 = frcp(ln1 + 2.0f * mn1);
             const float rm0 = frcp(mn0), rm1 = frcp(mn1);
             const float rl2 = zrow<2>(rl0, rl1), rm2 = zrow<2>(rm0, rm1);
@@ -223,8 +259,8 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
         float v10, v11, v40, v41;
         {
             float t0, t1, s0, s1;
-            dz_coll<NO>(uz0, uz1, t0, t1);
-            dz_coll<NO>(ux0, ux1, s0, s1);
+            zc_coll<NO>(zz, t0, t1);
+            zc_coll<NO>(zx, s0, s1);
             v10 = ln0 * t0 * rdz * rdx; v11 = ln1 * t1 * rdz * rdx;
             v40 = mn0 * s0 * rdz * rdx; v41 = mn1 * s1 * rdz * rdx;
         }
