@@ -35,7 +35,8 @@ struct fdfk_batch {
     int* d_live = nullptr;
     int* d_edge_off = nullptr;
     int* d_march_off = nullptr;
-    int edge_blocks = 0, march_blocks = 0;
+    int* d_frame_off = nullptr;
+    int edge_blocks = 0, march_blocks = 0, frame_blocks = 0;
     size_t smem = 0;
     bool dirty = true;         // tables do not match the members
     bool in_flight = false;    // device state newer than the members' host state
@@ -62,9 +63,9 @@ void drop_graph(fdfk_batch* b)
 void free_tables(fdfk_batch* b)
 {
     cudaFree(b->d_args); cudaFree(b->d_march); cudaFree(b->d_dyn); cudaFree(b->d_live);
-    cudaFree(b->d_edge_off); cudaFree(b->d_march_off);
+    cudaFree(b->d_edge_off); cudaFree(b->d_march_off); cudaFree(b->d_frame_off);
     b->d_args = nullptr; b->d_march = nullptr; b->d_dyn = nullptr; b->d_live = nullptr;
-    b->d_edge_off = nullptr; b->d_march_off = nullptr;
+    b->d_edge_off = nullptr; b->d_march_off = nullptr; b->d_frame_off = nullptr;
     b->cap = 0;
 }
 
@@ -78,6 +79,7 @@ BatchTab table(const fdfk_batch* b)
     t.live = b->d_live;
     t.edge_off = b->d_edge_off;
     t.march_off = b->d_march_off;
+    t.frame_off = b->d_frame_off;
     return t;
 }
 
@@ -115,6 +117,7 @@ int rebuild(fdfk_batch* b)
         if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_live, cap * sizeof(int));
         if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_edge_off, (cap + 1) * sizeof(int));
         if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_march_off, (cap + 1) * sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_frame_off, (cap + 1) * sizeof(int));
         if (e != cudaSuccess) {
             free_tables(b);
             return set_error(FDFK_ENOMEM, std::string("batch tables: ") + cudaGetErrorString(e));
@@ -124,7 +127,7 @@ int rebuild(fdfk_batch* b)
     std::vector<StepArgs> args(n);
     std::vector<MarchArgs> march(n);
     std::vector<BatchDyn> dyn(n);
-    std::vector<int> live(n, 0), eoff(n + 1, 0), moff(n + 1, 0);
+    std::vector<int> live(n, 0), eoff(n + 1, 0), moff(n + 1, 0), foff(n + 1, 0);
     size_t smem = 0;
     // fast-path segments re-planned for the whole batch: about two waves of resident warps over
     // all members' work, 16..48 columns per segment (a member alone plans for itself only)
@@ -164,6 +167,7 @@ int rebuild(fdfk_batch* b)
         const int nsb = sample_blocks(s->nrcv);
         eoff[i + 1] = eoff[i] + a.n_tiles + nsb;
         moff[i + 1] = moff[i] + (m.n_bands * m.n_segs + 3) / 4;
+        foff[i + 1] = foff[i] + (m.n_bands > 0 ? frame_blocks(a) : 0);
         smem = std::max(smem, step_smem_for(a));
     }
     if (n) {
@@ -173,21 +177,24 @@ int rebuild(fdfk_batch* b)
         BK(cudaMemcpy(b->d_live, live.data(), n * sizeof(int), cudaMemcpyHostToDevice));
         BK(cudaMemcpy(b->d_edge_off, eoff.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
         BK(cudaMemcpy(b->d_march_off, moff.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        BK(cudaMemcpy(b->d_frame_off, foff.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
     }
     b->edge_blocks = eoff[n];
     b->march_blocks = moff[n];
+    b->frame_blocks = foff[n];
     b->smem = smem;
     // opt the batched kernels into their shared memory outside any stream capture
     const BatchTab t = table(b);
     if (n) {
         BK(launch_step_batch(t, b->norder, 0, b->smem, b->stream));
-        if (b->norder <= kMarchMaxOrder) BK(launch_march_batch(t, b->norder, 0, b->stream));
+        if (b->norder <= kMarchMaxOrder) BK(launch_march_batch(t, b->norder, 0, 0, b->stream));
     }
     b->dirty = false;
     return FDFK_OK;
 }
 
-// One step of every live member: bump, then the two kernels on two streams.
+// One step of every live member: bump, then the tiled kernel on the side stream next to the
+// frames and the fast path on the main stream.
 cudaError_t step_once(fdfk_batch* b)
 {
     const BatchTab t = table(b);
@@ -196,13 +203,14 @@ cudaError_t step_once(fdfk_batch* b)
     if ((e = cudaEventRecord(b->fork, b->stream)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(b->side, b->fork, 0)) != cudaSuccess) return e;
     if ((e = launch_step_batch(t, b->norder, b->edge_blocks, b->smem, b->side)) != cudaSuccess) return e;
-    if (b->march_blocks > 0 && (e = launch_march_batch(t, b->norder, b->march_blocks, b->stream)) != cudaSuccess)
+    if (b->march_blocks > 0 &&
+        (e = launch_march_batch(t, b->norder, b->frame_blocks, b->march_blocks, b->stream)) != cudaSuccess)
         return e;
     if ((e = cudaEventRecord(b->join, b->side)) != cudaSuccess) return e;
     return cudaStreamWaitEvent(b->stream, b->join, 0);
 }
 
-int launches_per_step(const fdfk_batch* b) { return 2 + (b->march_blocks > 0 ? 1 : 0); }
+int launches_per_step(const fdfk_batch* b) { return 2 + (b->march_blocks > 0 ? 2 : 0); }
 
 }  // namespace
 

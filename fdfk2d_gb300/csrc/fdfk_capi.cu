@@ -136,6 +136,7 @@ void free_session(fdfk_session* s)
     if (s->join) cudaEventDestroy(s->join);
     cudaFree(s->kdt2); cudaFree(s->lam); cudaFree(s->mu);
     for (int l = 0; l < 2; ++l) { cudaFree(s->ux[l]); cudaFree(s->uz[l]); }
+    cudaFree(s->fux); cudaFree(s->fuz);
     for (int k = 0; k < 24; ++k) for (int l = 0; l < 2; ++l) cudaFree(s->bu[k][l]);
     for (int k = 0; k < 12; ++k) cudaFree(s->bp[k]);
     cudaFree(s->dampx); cudaFree(s->dampz);
@@ -205,6 +206,8 @@ int zero_state(fdfk_session* s)
         CK(cudaMemsetAsync(s->ux[l], 0, n * sizeof(float), s->stream));
         CK(cudaMemsetAsync(s->uz[l], 0, n * sizeof(float), s->stream));
     }
+    if (s->fux) CK(cudaMemsetAsync(s->fux, 0, n * sizeof(float), s->stream));   // rows never written stay 0
+    if (s->fuz) CK(cudaMemsetAsync(s->fuz, 0, n * sizeof(float), s->stream));
     for (int k = 0; k < 24; ++k)
         for (int l = 0; l < 2; ++l)
             if (s->bu[k][l]) CK(cudaMemsetAsync(s->bu[k][l], 0, bu_elems(s->p, k) * sizeof(float), s->stream));
@@ -248,7 +251,10 @@ int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out
     s->p = *p;
     s->NZ = p->nz + p->npml;
     s->NX = p->nx + 2 * p->npml;
-    s->ldz = (s->NZ + 31) / 32 * 32;
+    // FDFK_TILED_ONLY=1 keeps every cell on the tiled kernel (used to cross-check the two paths).
+    const char* tiled_only = std::getenv("FDFK_TILED_ONLY");
+    const bool march = p->norder <= kMarchMaxOrder && p->nz >= 2 * p->norder + 1 && !(tiled_only && tiled_only[0] == '1');
+    s->ldz = plane_ldz(p->nz, p->npml, p->norder, march);
     const size_t n = (size_t)s->ldz * s->NX;
 
     auto alloc = [&](void** ptr, size_t bytes) -> int {
@@ -263,6 +269,7 @@ int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out
     AL(s->lam, n * sizeof(float));
     AL(s->mu, n * sizeof(float));
     for (int l = 0; l < 2; ++l) { AL(s->ux[l], n * sizeof(float)); AL(s->uz[l], n * sizeof(float)); }
+    if (march) { AL(s->fux, n * sizeof(float)); AL(s->fuz, n * sizeof(float)); }
     for (int k = 0; k < 18; ++k)          // l, r, b (the top PML is not used with a free surface)
         for (int l = 0; l < 2; ++l) AL(s->bu[k][l], bu_elems(*p, k) * sizeof(float));
     for (int k = 0; k < 12; ++k)
@@ -299,11 +306,9 @@ int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out
     a.kdt2 = s->kdt2; a.lam = s->lam; a.mu = s->mu;
     a.dampx = s->dampx; a.dampz = s->dampz;
     for (int k = 0; k < NSTRIP; ++k) a.strip[k] = s->strip[k];
+    a.fux = s->fux; a.fuz = s->fuz;
     // Interior rows from 2*norder+1 down go to the marching fast path (orders <= kMarchMaxOrder): below
     // them every stencil has its full order.
-    // FDFK_TILED_ONLY=1 keeps every cell on the tiled kernel (used to cross-check the two paths).
-    const char* tiled_only = std::getenv("FDFK_TILED_ONLY");
-    const bool march = p->norder <= kMarchMaxOrder && p->nz >= 2 * p->norder + 1 && !(tiled_only && tiled_only[0] == '1');
     a.int_rows = march ? 2 * p->norder : p->nz;
     s->march.z0 = 2 * p->norder + 1;
     s->march.band_out = 64 - 4 * p->norder;
@@ -437,7 +442,7 @@ int fdfk_session_advance(fdfk_session* s, int nsteps)
             if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("march launch: ") + cudaGetErrorString(e));
             CK(cudaEventRecord(s->join, s->side));
             CK(cudaStreamWaitEvent(s->stream, s->join, 0));
-            g_launches.fetch_add(nl + 1);
+            g_launches.fetch_add(nl + 2);
         } else {
             cudaError_t e = launch_step(a, s->stream);
             if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("step launch: ") + cudaGetErrorString(e));
@@ -496,7 +501,7 @@ int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, 
             cudaStreamWaitEvent(s->stream, s->join, 0);
         }
         if (r != cudaSuccess) { cleanup(); return fail(FDFK_ECUDA, std::string("launch: ") + cudaGetErrorString(r)); }
-        g_launches.fetch_add(nl + (two ? 1 : 0));
+        g_launches.fetch_add(nl + (two ? 2 : 0));
         s->cur ^= 1;
         s->it += 1;
     }

@@ -141,18 +141,73 @@ __device__ __forceinline__ void march_warp(const StepArgs& a, const MarchArgs& m
     const int b = m.z0 + band * m.band_out - 2 * NO;   // first row of the band
     const int xs = 1 + seg * m.seg_len;
     const int xe = min(a.nx, xs + m.seg_len - 1);
-    // warp-uniform: does the segment's column reach (xs-3NO+1 .. xe+2NO) leave 1..nx, does the band
-    // (rows b .. b+63) pass nz
-    const bool ex = xs - 3 * NO + 1 < 1 || xe + 2 * NO > a.nx;
-    const bool ez = b + 63 > a.nz;
     float* ring = ring_smem + (size_t)wib * march::Ring<NO>::kWarpFloats;
-    if (ex) {
-        if (ez) march::march_ring<NO, true, true>(a, m, lane, b, xs, xe, ring);
-        else march::march_ring<NO, true, false>(a, m, lane, b, xs, xe, ring);
+    march::march_ring<NO>(a, m, lane, b, xs, xe, ring);
+}
+
+// ---------------------------------------------------------------------------
+// The frame of a step: u^n plus the outer background (Omega_II, as the tiled
+// kernel injects it) at every cell the fast path reads outside the regular
+// domain -- columns 1-nbd..0 and nx+1..nx+nbd on rows 1..NZ, and rows
+// nz..nz+nbd of columns 1..nx (row nz carries no background; it is copied so
+// that a lane whose rows straddle nz reads both from the frame).  nbd =
+// 2*norder-1 is the reach of the fast path's stencils.  Written before the
+// march of the step, read only by it.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline long long frame_cells(const StepArgs& a)
+{
+    return 2LL * a.nbd * a.NZ + (long long)(a.nbd + 1) * a.nx;
+}
+
+__device__ __forceinline__ void frame_cell(const StepArgs& a, long long i)
+{
+    const int nbd = a.nbd, NZ = a.NZ, nx = a.nx;
+    const long long sidec = (long long)nbd * NZ;
+    int iz, ix;
+    if (i < 2 * sidec) {
+        const bool right = i >= sidec;
+        const long long j = right ? i - sidec : i;
+        const int c = (int)(j / NZ);
+        iz = (int)(j - (long long)c * NZ) + 1;
+        ix = right ? nx + 1 + c : 1 - nbd + c;
     } else {
-        if (ez) march::march_ring<NO, false, true>(a, m, lane, b, xs, xe, ring);
-        else march::march_ring<NO, false, false>(a, m, lane, b, xs, xe, ring);
+        const long long j = i - 2 * sidec;
+        if (j >= (long long)(nbd + 1) * nx) return;
+        const int c = (int)(j / (nbd + 1));
+        iz = a.nz + (int)(j - (long long)c * (nbd + 1));
+        ix = 1 + c;
     }
+    const size_t g = gidx(a, iz, ix);
+    float vx = a.ux[a.cur][g], vz = a.uz[a.cur][g];
+    const float* pz = nullptr;
+    const float* px = outer_bg_ptr(a, iz, ix, pz);
+    if (px) {
+        vx += __ldg(px);
+        vz += __ldg(pz);
+    }
+    a.fux[g] = vx;
+    a.fuz[g] = vz;
+}
+
+constexpr int kFrameThreads = 256;
+
+__global__ void __launch_bounds__(kFrameThreads) fdfk_frame_kernel(StepArgs a)
+{
+    frame_cell(a, (long long)blockIdx.x * kFrameThreads + threadIdx.x);
+}
+
+// The frames of every live member of a batch: member s owns blocks frame_off[s] .. frame_off[s+1]-1.
+__global__ void __launch_bounds__(kFrameThreads) fdfk_frame_batch_kernel(BatchTab t)
+{
+    const int s = batch_member(t.frame_off, t.n, blockIdx.x);
+    if (!t.live[s]) return;
+    frame_cell(t.args[s], (long long)(blockIdx.x - t.frame_off[s]) * kFrameThreads + threadIdx.x);
+}
+
+// Blocks of one member's frame launch.
+int frame_blocks(const StepArgs& a)
+{
+    return (int)((frame_cells(a) + kFrameThreads - 1) / kFrameThreads);
 }
 
 template <int NO>
@@ -233,7 +288,21 @@ static cudaError_t launch_march_batch_no(const BatchTab& t, int blocks, cudaStre
     return cudaGetLastError();
 }
 
-cudaError_t launch_march_batch(const BatchTab& t, int norder, int blocks, cudaStream_t s)
+cudaError_t launch_march_batch_fast(const BatchTab& t, int norder, int blocks, cudaStream_t s);
+
+// The frames of a batch (frame_blocks blocks), then its fast path (blocks blocks); 0 blocks only
+// opts the kernel into its shared memory.
+cudaError_t launch_march_batch(const BatchTab& t, int norder, int frame_blocks_total, int blocks, cudaStream_t s)
+{
+    if (blocks > 0 && frame_blocks_total > 0) {
+        fdfk_frame_batch_kernel<<<frame_blocks_total, kFrameThreads, 0, s>>>(t);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return launch_march_batch_fast(t, norder, blocks, s);
+}
+
+cudaError_t launch_march_batch_fast(const BatchTab& t, int norder, int blocks, cudaStream_t s)
 {
     switch (norder) {
     case 1: return launch_march_batch_no<1>(t, blocks, s);
@@ -244,9 +313,13 @@ cudaError_t launch_march_batch(const BatchTab& t, int norder, int blocks, cudaSt
     }
 }
 
+// The frame of the step, then the fast path (two launches).
 cudaError_t launch_march(const StepArgs& a, const MarchArgs& m, cudaStream_t s)
 {
     if (m.n_bands <= 0 || m.n_segs <= 0) return cudaSuccess;
+    fdfk_frame_kernel<<<frame_blocks(a), kFrameThreads, 0, s>>>(a);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     switch (a.norder) {
     case 1: return launch_march_no<1>(a, m, s);
     case 2: return launch_march_no<2>(a, m, s);

@@ -1,12 +1,6 @@
 // The march of one warp, fed by asynchronous copies (included inside
 // namespace fdfk::march by fdfk_march.cuh).
 //
-// EX: the segment's columns (with the stencil reach) leave 1..nx (background
-// strips, PML columns, columns beyond the grid); EZ: the band passes row nz
-// (bottom strip rows, rows beyond the grid).  Values outside the grid are
-// written into the ring directly (u = 0, lambda = 0, mu = 1); the Omega_II
-// background is added to the register copies of u after the ring read, so the
-// ring keeps the raw u^n for the time update.
 // Each lane copies its own two rows of every field with cp.async into a
 // per-warp shared-memory ring, kAhead columns before they are used, so the
 // DRAM latency is covered by the march itself instead of by registers.
@@ -16,7 +10,13 @@
 //   ring B: dt^2/rho and u^{n-1} of the cell emitted kAhead columns later.
 // A lane only reads back what it copied itself, so cp.async.wait_group is the
 // only synchronisation (no barrier, no spin loop).
-
+//
+// Every warp runs the same code.  Outside the regular domain (columns outside
+// 1..nx, rows from nz down) u is read from the step's frame (StepArgs::fux,
+// fuz: u^n with the Omega_II background already added, written by
+// fdfk_frame_kernel); rows past NZ are padding rows of the planes (u = 0,
+// lambda = 0, mu = 1); material columns left of the grid (npml < 3NO-1 only)
+// are written into the ring as those constants.
 template <int NO>
 struct Ring {
     static constexpr int kAhead = 2;                            // columns fetched ahead of use
@@ -42,6 +42,11 @@ template <int OFF>
 __device__ __forceinline__ void cp_async8_s(unsigned s, const float* g)
 {
     asm volatile("cp.async.ca.shared.global [%0+%2], [%1], 8;\n" ::"r"(s), "l"(g), "n"(OFF) : "memory");
+}
+template <int OFF>
+__device__ __forceinline__ void cp_async4_s(unsigned s, const float* g)
+{
+    asm volatile("cp.async.ca.shared.global [%0+%2], [%1], 4;\n" ::"r"(s), "l"(g), "n"(OFF) : "memory");
 }
 // z-derivatives of one shuffled column (rows r0-NO .. r0+NO+1), shared by the staggered and
 // the collocated stencils of the same field.
@@ -70,7 +75,7 @@ __device__ __forceinline__ void zc_coll(const ZCol<-NO, NO + 1>& z, float& d0, f
     d1 = s1;
 }
 
-template <int NO, bool EX, bool EZ>
+template <int NO>
 __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m, int lane, int b, int xs, int xe,
                                            float* ring)
 {
@@ -81,17 +86,17 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
     constexpr int LAG = 2 * NO - 1;  // newest column minus completed cell
 
     const int r0 = b + 2 * lane;
-    const int nx = a.nx, nz = a.nz, NZ = a.NZ, npml = a.npml, ldz = a.ldz, nbd = a.nbd, it = a.it;
+    const int nx = a.nx, nz = a.nz, npml = a.npml, ldz = a.ldz;
     const bool store = lane >= NO && lane <= 31 - NO && r0 >= m.z0 && r0 <= nz;
-    const bool store1 = store && (!EZ || r0 + 1 <= nz);
-    const bool rows_in = !EZ || (r0 >= 1 && r0 + 1 <= NZ);
-    const bool r0_in = r0 >= 1 && r0 <= NZ, r1_in = r0 + 1 >= 1 && r0 + 1 <= NZ;
-    const bool r1_int = !EZ || r0 + 1 <= nz;
+    const bool store1 = store && r0 + 1 <= nz;
+    const bool lane_frame = r0 + 1 > nz;       // both rows from the frame (row nz is copied there)
 
     const float* __restrict__ uxc = a.ux[a.cur];
     const float* __restrict__ uzc = a.uz[a.cur];
     float* __restrict__ uxn = a.ux[a.cur ^ 1];
     float* __restrict__ uzn = a.uz[a.cur ^ 1];
+    const float* const uxl = lane_frame ? a.fux : uxc;    // u source of this lane inside columns 1..nx
+    const float* const uzl = lane_frame ? a.fuz : uzc;
     const float rdx = 1.0f / a.dx, rdz = 1.0f / a.dz;
     const float dx2 = a.dx2r, dz2 = a.dz2;
 
@@ -115,64 +120,37 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
     // one commit group per column; ring B of column col holds the cell col - LAG
     auto issue = [&](int col) {
         if (col <= m1) {
-            if (EX && (col < 1 - npml || col > nx + npml)) {
+            if (col < 1 - npml) {               // left of the grid (only the lagged material is used)
                 st_shared2(slotA(col, 0), 0.f, 0.f);
                 st_shared2(slotA(col, 1), 0.f, 0.f);
                 st_shared2(slotA(col, 2), 0.f, 0.f);
                 st_shared2(slotA(col, 3), 1.f, 1.f);
             } else {
                 const int o = gofs(col);
-                if (rows_in) {
-                    const unsigned sa = sA(col);
-                    cp_async8_s<0 * kFA>(sa, uxc + o);
-                    cp_async8_s<1 * kFA>(sa, uzc + o);
-                    cp_async8_s<2 * kFA>(sa, a.lam + o);
-                    cp_async8_s<3 * kFA>(sa, a.mu + o);
-                } else {   // a lane straddling the bottom of the grid: rows outside read as u = lambda = 0, mu = 1
-                    st_shared2(slotA(col, 0), r0_in ? __ldg(uxc + o) : 0.f, r1_in ? __ldg(uxc + o + 1) : 0.f);
-                    st_shared2(slotA(col, 1), r0_in ? __ldg(uzc + o) : 0.f, r1_in ? __ldg(uzc + o + 1) : 0.f);
-                    st_shared2(slotA(col, 2), r0_in ? __ldg(a.lam + o) : 0.f, r1_in ? __ldg(a.lam + o + 1) : 0.f);
-                    st_shared2(slotA(col, 3), r0_in ? __ldg(a.mu + o) : 1.f, r1_in ? __ldg(a.mu + o + 1) : 1.f);
-                }
+                const bool fr = col < 1 || col > nx;
+                const unsigned sa = sA(col);
+                cp_async8_s<0 * kFA>(sa, (fr ? a.fux : uxl) + o);
+                cp_async8_s<1 * kFA>(sa, (fr ? a.fuz : uzl) + o);
+                cp_async8_s<2 * kFA>(sa, a.lam + o);
+                cp_async8_s<3 * kFA>(sa, a.mu + o);
             }
             const int xcol = col - LAG;
             if (store && xcol >= xs) {
                 const int oc = gofs(xcol);
+                const unsigned sb = sB(col);
                 if (store1) {
-                    const unsigned sb = sB(col);
                     cp_async8_s<0 * kFB>(sb, a.kdt2 + oc);
                     cp_async8_s<1 * kFB>(sb, uxn + oc);
                     cp_async8_s<2 * kFB>(sb, uzn + oc);
-                } else {
-                    st_shared2(slotB(col, 0), __ldg(a.kdt2 + oc), 0.f);
-                    st_shared2(slotB(col, 1), uxn[oc], 0.f);
-                    st_shared2(slotB(col, 2), uzn[oc], 0.f);
+                } else {   // only row r0 (= nz) is stored
+                    cp_async4_s<0 * kFB>(sb, a.kdt2 + oc);
+                    cp_async4_s<1 * kFB>(sb, uxn + oc);
+                    cp_async4_s<2 * kFB>(sb, uzn + oc);
+                    slotB(col, 0)[1] = 0.f; slotB(col, 1)[1] = 0.f; slotB(col, 2)[1] = 0.f;
                 }
             }
         }
         cp_commit();
-    };
-    // Omega_II background of column ix added to the register copy of u^n (columns outside 1..nx, rows below nz)
-    auto inject = [&](int ix, float& x0, float& x1, float& z0, float& z1) {
-        if (EX && ((ix <= 0 && ix >= 1 - nbd) || (ix > nx && ix <= nx + nbd)) && r0 <= nz) {
-            const bool left = ix <= 0;
-            const size_t so = (size_t)(r0 - 1) + (size_t)nz * ((size_t)(left ? ix - (1 - nbd) : ix - nx - 1) + (size_t)nbd * it);
-            const float* sx = a.strip[left ? UXL_PML : UXR_PML] + so;
-            const float* sz = a.strip[left ? UZL_PML : UZR_PML] + so;
-            x0 += __ldg(sx); z0 += __ldg(sz);
-            if (r1_int) { x1 += __ldg(sx + 1); z1 += __ldg(sz + 1); }
-        }
-        if (EZ && r0 + 1 > nz && ix >= 1 - nbd && ix <= nx + nbd) {
-            const size_t cb = (size_t)(nx + 2 * nbd) * it + (size_t)(ix - (1 - nbd));
-            if (r0 >= nz + 1 && r0 <= nz + nbd) {
-                const size_t so = (size_t)(r0 - nz - 1) + (size_t)nbd * cb;
-                x0 += __ldg(a.strip[UXB_PML] + so); z0 += __ldg(a.strip[UZB_PML] + so);
-            }
-            if (r0 + 1 >= nz + 1 && r0 + 1 <= nz + nbd) {
-                const size_t so = (size_t)(r0 - nz) + (size_t)nbd * cb;
-                x1 += __ldg(a.strip[UXB_PML] + so); z1 += __ldg(a.strip[UZB_PML] + so);
-            }
-        }
     };
     for (int c = c0; c < m0 + RG::kAhead; ++c) issue(c);
     cp_wait<RG::kAhead>();                      // columns c0 .. m0-1 have landed
@@ -200,8 +178,7 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
         cp_wait<RG::kAhead>();                  // column mc has landed
         const float2 U = rdA(mc, 0), Z = rdA(mc, 1), LNv = rdA(mc, 2), MNv = rdA(mc, 3);
         const float2 LQv = rdA(mc - NO + 1, 2), MQv = rdA(mc - NO + 1, 3);
-        float ux0 = U.x, ux1 = U.y, uz0 = Z.x, uz1 = Z.y;
-        if (EX || EZ) inject(mc, ux0, ux1, uz0, uz1);
+        const float ux0 = U.x, ux1 = U.y, uz0 = Z.x, uz1 = Z.y;
         const float ln0 = LNv.x, ln1 = LNv.y, mn0 = MNv.x, mn1 = MNv.y;
         const float lq0 = LQv.x, lq1 = LQv.y, mq0 = MQv.x, mq1 = MQv.y;
         const int xc = mc - LAG;

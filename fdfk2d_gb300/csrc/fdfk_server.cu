@@ -97,12 +97,13 @@ extern "C" {
 long long fdfk_session_device_bytes(const fdfk_params* p, int nrcv, int nsis)
 {
     if (!p || p->nx < 1 || p->nz < 1 || p->npml < 0 || p->nt < 0 || nrcv < 0) return -1;
-    const long long NZ = p->nz + p->npml, NX = p->nx + 2LL * p->npml, ldz = (NZ + 31) / 32 * 32;
+    const bool fast = p->norder <= kMarchMaxOrder && p->nz >= 2 * p->norder + 1;
+    const long long NZ = p->nz + p->npml, NX = p->nx + 2LL * p->npml, ldz = plane_ldz(p->nz, p->npml, p->norder, fast);
     const long long n = ldz * NX;
     const long long side = (long long)p->nz * p->npml, tb = (long long)p->npml * NX;
     const long long nx = p->nx, nz = p->nz, nbd = p->nbd;
     const long long strips = 4 * (nz - nbd) * nbd + 2 * nbd * nx + 4 * nz * nbd + 2 * nbd * (nx + 2 * nbd);
-    long long f = 7 * n + 2 * (12 * side + 6 * tb) + 4 * side + 4 * tb + strips * (p->nt + 1LL);
+    long long f = (fast ? 9 : 7) * n + 2 * (12 * side + 6 * tb) + 4 * side + 4 * tb + strips * (p->nt + 1LL);
     f += 2LL * nrcv + (nrcv > 0 ? 2LL * (nsis + 1) * nrcv : 0);
     return 4 * f + (long long)sizeof(DampCol) * (NX + NZ);
 }

@@ -21,6 +21,8 @@ struct fdfk_session {
     float* mu = nullptr;
     float* ux[2] = {nullptr, nullptr};
     float* uz[2] = {nullptr, nullptr};
+    float* fux = nullptr;   // frame of the fast path (allocated when it runs)
+    float* fuz = nullptr;
     float* bu[24][2] = {};
     float* bp[12] = {};
     fdfk::DampCol* dampx = nullptr;

@@ -81,43 +81,51 @@ __device__ __forceinline__ size_t gidx(const StepArgs& a, int iz, int ix)
     return (size_t)(iz - 1) + (size_t)(ix + a.npml - 1) * (size_t)a.ldz;
 }
 
-// Background value at (iz, ix) on the outer strips (Omega_II), or 0.
-__device__ __forceinline__ void outer_bg(const StepArgs& a, int iz, int ix, float& bx, float& bz)
+// Address of the background at (iz, ix) on the outer strips (Omega_II): the x component,
+// with the z component in pz; nullptr where there is none.
+__device__ __forceinline__ const float* outer_bg_ptr(const StepArgs& a, int iz, int ix, const float*& pz)
 {
     const int nx = a.nx, nz = a.nz, nbd = a.nbd, it = a.it;
-    bx = 0.f; bz = 0.f;
     if (iz >= 1 && iz <= nz) {
         if (ix >= 1 - nbd && ix <= 0) {
-            size_t o = (size_t)(iz - 1) + (size_t)nz * ((size_t)(ix - (1 - nbd)) + (size_t)nbd * it);
-            bx = __ldg(a.strip[UXL_PML] + o); bz = __ldg(a.strip[UZL_PML] + o);
-        } else if (ix >= nx + 1 && ix <= nx + nbd) {
-            size_t o = (size_t)(iz - 1) + (size_t)nz * ((size_t)(ix - nx - 1) + (size_t)nbd * it);
-            bx = __ldg(a.strip[UXR_PML] + o); bz = __ldg(a.strip[UZR_PML] + o);
+            const size_t o = (size_t)(iz - 1) + (size_t)nz * ((size_t)(ix - (1 - nbd)) + (size_t)nbd * it);
+            pz = a.strip[UZL_PML] + o;
+            return a.strip[UXL_PML] + o;
+        }
+        if (ix >= nx + 1 && ix <= nx + nbd) {
+            const size_t o = (size_t)(iz - 1) + (size_t)nz * ((size_t)(ix - nx - 1) + (size_t)nbd * it);
+            pz = a.strip[UZR_PML] + o;
+            return a.strip[UXR_PML] + o;
         }
     } else if (iz >= nz + 1 && iz <= nz + nbd && ix >= 1 - nbd && ix <= nx + nbd) {
-        size_t o = (size_t)(iz - nz - 1) + (size_t)nbd * ((size_t)(ix - (1 - nbd)) + (size_t)(nx + 2 * nbd) * it);
-        bx = __ldg(a.strip[UXB_PML] + o); bz = __ldg(a.strip[UZB_PML] + o);
+        const size_t o = (size_t)(iz - nz - 1) + (size_t)nbd * ((size_t)(ix - (1 - nbd)) + (size_t)(nx + 2 * nbd) * it);
+        pz = a.strip[UZB_PML] + o;
+        return a.strip[UXB_PML] + o;
     }
+    return nullptr;
 }
 
-// Background value at (iz, ix) on the inner strips (Omega_I), or 0.
-__device__ __forceinline__ void inner_bg(const StepArgs& a, int iz, int ix, float& bx, float& bz)
+// Address of the background at (iz, ix) on the inner strips (Omega_I), as outer_bg_ptr.
+__device__ __forceinline__ const float* inner_bg_ptr(const StepArgs& a, int iz, int ix, const float*& pz)
 {
     const int nx = a.nx, nz = a.nz, nbd = a.nbd, it = a.it;
-    bx = 0.f; bz = 0.f;
-    if (ix < 1 || ix > nx || iz < 1 || iz > nz) return;
+    if (ix < 1 || ix > nx || iz < 1 || iz > nz) return nullptr;
     if (iz <= nz - nbd) {
         if (ix <= nbd) {
-            size_t o = (size_t)(iz - 1) + (size_t)(nz - nbd) * ((size_t)(ix - 1) + (size_t)nbd * it);
-            bx = __ldg(a.strip[UXL_REG] + o); bz = __ldg(a.strip[UZL_REG] + o);
-        } else if (ix >= nx - nbd + 1) {
-            size_t o = (size_t)(iz - 1) + (size_t)(nz - nbd) * ((size_t)(ix - (nx - nbd + 1)) + (size_t)nbd * it);
-            bx = __ldg(a.strip[UXR_REG] + o); bz = __ldg(a.strip[UZR_REG] + o);
+            const size_t o = (size_t)(iz - 1) + (size_t)(nz - nbd) * ((size_t)(ix - 1) + (size_t)nbd * it);
+            pz = a.strip[UZL_REG] + o;
+            return a.strip[UXL_REG] + o;
         }
-    } else {
-        size_t o = (size_t)(iz - (nz - nbd + 1)) + (size_t)nbd * ((size_t)(ix - 1) + (size_t)nx * it);
-        bx = __ldg(a.strip[UXB_REG] + o); bz = __ldg(a.strip[UZB_REG] + o);
+        if (ix >= nx - nbd + 1) {
+            const size_t o = (size_t)(iz - 1) + (size_t)(nz - nbd) * ((size_t)(ix - (nx - nbd + 1)) + (size_t)nbd * it);
+            pz = a.strip[UZR_REG] + o;
+            return a.strip[UXR_REG] + o;
+        }
+        return nullptr;
     }
+    const size_t o = (size_t)(iz - (nz - nbd + 1)) + (size_t)nbd * ((size_t)(ix - 1) + (size_t)nx * it);
+    pz = a.strip[UZB_REG] + o;
+    return a.strip[UXB_REG] + o;
 }
 
 __device__ __forceinline__ Rect decode_tile(const StepArgs& a, int b)
@@ -245,40 +253,67 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
     const float* uzc = a.uz[a.cur];
 
     // ---- phase 0: field tile (with injection) and material tile -------------
-    for (int i = tid; i < T.U; i += kThreads) {
-        int sz = i % T.UZ, sx = i / T.UZ;
-        int iz = R.z0 - H + sz, ix = R.x0 - H + sx;
-        float vx = 0.f, vz = 0.f;
-        if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
-            size_t g = gidx(a, iz, ix);
-            vx = uxc[g];
-            vz = uzc[g];
-            float bx, bz;
-            if (!pml) {
-                outer_bg(a, iz, ix, bx, bz);
-                vx += bx; vz += bz;
-            } else {
-                inner_bg(a, iz, ix, bx, bz);
-                vx -= bx; vz -= bz;
+    // kFill items per thread per round: every load of a round is issued before the first
+    // shared-memory store, so a round costs one memory latency.
+    constexpr int kFill = 4;
+    for (int i0 = tid; i0 < T.U; i0 += kFill * kThreads) {
+        float vx[kFill], vz[kFill], bx[kFill], bz[kFill];
+#pragma unroll
+        for (int q = 0; q < kFill; ++q) {
+            const int i = i0 + q * kThreads;
+            vx[q] = 0.f; vz[q] = 0.f; bx[q] = 0.f; bz[q] = 0.f;
+            if (i < T.U) {
+                const int sz = i % T.UZ, sx = i / T.UZ;
+                const int iz = R.z0 - H + sz, ix = R.x0 - H + sx;
+                if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
+                    const size_t g = gidx(a, iz, ix);
+                    vx[q] = uxc[g];
+                    vz[q] = uzc[g];
+                    const float* pz = nullptr;
+                    const float* px = pml ? inner_bg_ptr(a, iz, ix, pz) : outer_bg_ptr(a, iz, ix, pz);
+                    if (px) {
+                        bx[q] = __ldg(px);
+                        bz[q] = __ldg(pz);
+                    }
+                }
             }
         }
-        sux[i] = vx;
-        suz[i] = vz;
-    }
-    for (int i = tid; i < T.M; i += kThreads) {
-        int mz = i % T.MZ, mx = i / T.MZ;
-        int iz = R.z0 - NO + mz, ix = R.x0 - NO + mx;
-        float l = 0.f, m = 1.f;
-        if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
-            size_t g = gidx(a, iz, ix);
-            l = __ldg(a.lam + g);
-            m = __ldg(a.mu + g);
+#pragma unroll
+        for (int q = 0; q < kFill; ++q) {
+            const int i = i0 + q * kThreads;
+            if (i < T.U) {
+                sux[i] = pml ? vx[q] - bx[q] : vx[q] + bx[q];
+                suz[i] = pml ? vz[q] - bz[q] : vz[q] + bz[q];
+            }
         }
-        float l2 = l + 2.0f * m;
-        sLam[i] = l;
-        sMu[i] = m;
-        sRL2m[i] = fast_rcp(l2);
-        sRMu[i] = fast_rcp(m);
+    }
+    for (int i0 = tid; i0 < T.M; i0 += kFill * kThreads) {
+        float l[kFill], m[kFill];
+#pragma unroll
+        for (int q = 0; q < kFill; ++q) {
+            const int i = i0 + q * kThreads;
+            l[q] = 0.f; m[q] = 1.f;
+            if (i < T.M) {
+                const int mz = i % T.MZ, mx = i / T.MZ;
+                const int iz = R.z0 - NO + mz, ix = R.x0 - NO + mx;
+                if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
+                    const size_t g = gidx(a, iz, ix);
+                    l[q] = __ldg(a.lam + g);
+                    m[q] = __ldg(a.mu + g);
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kFill; ++q) {
+            const int i = i0 + q * kThreads;
+            if (i < T.M) {
+                const float l2 = l[q] + 2.0f * m[q];
+                sLam[i] = l[q];
+                sMu[i] = m[q];
+                sRL2m[i] = fast_rcp(l2);
+                sRMu[i] = fast_rcp(m[q]);
+            }
+        }
     }
     __syncthreads();
 
@@ -390,6 +425,8 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             continue;
         }
 
+        const float kd = __ldg(a.kdt2 + g);
+
         // x-direction second derivatives dxx(l2m ux), dxx(mu uz)
         float x2a = 0.f, x2b = 0.f;
 #pragma unroll
@@ -491,7 +528,6 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             duz1 = 0.5f * (la1 * dx1 + la2 * dx2v);     // (lam1 Dx ux1 + lam2 Dx ux2)/2
         }
 
-        const float kd = __ldg(a.kdt2 + g);
         float* uxn = a.ux[a.cur ^ 1];
         float* uzn = a.uz[a.cur ^ 1];
         const float ux0 = uxc[g], uz0 = uzc[g];
@@ -511,15 +547,34 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         }
 
         // ---- PML cell: split-field update ----------------------------------
+        // Absorbing-layer state of the cell, gathered in one round of loads (in flight while the
+        // first derivatives below are formed) before any of it is written back.
         const int side = R.side;
-        const DampCol dxc = a.dampx[ix + npml - 1];
-        const DampCol dzc = side == 3 ? a.dampz[iz - 1] : DampCol{0.f, 0.f, 1.f, 1.f};
+        size_t ap = 0;
+        float gPx[2], gPz[2], gU1[2], gU1m[2], gU2[2], gU2m[2], gU3[2], gU3m[2];
+        DampCol dxc{0.f, 0.f, 1.f, 1.f}, dzc{0.f, 0.f, 1.f, 1.f};
+        {
+            if (side == 1) ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - (1 - npml));
+            else if (side == 2) ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - nx - 1);
+            else ap = (size_t)(iz - nz - 1) + (size_t)npml * (size_t)(ix - (1 - npml));
+            const int base = side == 1 ? 0 : side == 2 ? 6 : 12;
+            const int bpx0 = side == 1 ? 0 : side == 2 ? 2 : 8;
+#pragma unroll
+            for (int comp = 0; comp < 2; ++comp) {
+                gPx[comp] = a.bp[side == 3 ? bpx0 + 2 * comp : bpx0 + comp][ap];
+                gPz[comp] = side == 3 ? a.bp[9 + 2 * comp][ap] : 0.f;
+                gU1[comp] = a.bu[base + 3 * comp + 0][a.cur][ap];
+                gU1m[comp] = a.bu[base + 3 * comp + 0][a.cur ^ 1][ap];
+                gU2[comp] = a.bu[base + 3 * comp + 1][a.cur][ap];
+                gU2m[comp] = a.bu[base + 3 * comp + 1][a.cur ^ 1][ap];
+                gU3[comp] = a.bu[base + 3 * comp + 2][a.cur][ap];
+                gU3m[comp] = a.bu[base + 3 * comp + 2][a.cur ^ 1][ap];
+            }
+            dxc = a.dampx[ix + npml - 1];
+            if (side == 3) dzc = a.dampz[iz - 1];
+        }
         const float yx = dxc.y, yz = dzc.y;
         const float r2 = side == 3 ? fast_rcp(1.0f + 0.5f * (yx + yz)) : dxc.rh;   // 1 / (1 + (yx + yz)/2)
-        size_t ap;
-        if (side == 1) ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - (1 - npml));
-        else if (side == 2) ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - nx - 1);
-        else ap = (size_t)(iz - nz - 1) + (size_t)npml * (size_t)(ix - (1 - npml));
 
         // first derivatives for the memory variables (diff1 / diffx1 on the PML field)
         float dxux = 0.f, dxuz = 0.f, dzux = 0.f, dzuz = 0.f;
@@ -536,7 +591,7 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
 
         const int base = side == 1 ? 0 : side == 2 ? 6 : 12;
         const int bpx0 = side == 1 ? 0 : side == 2 ? 2 : 8;
-        const int plane = a.cur, nplane = a.cur ^ 1;
+        const int nplane = a.cur ^ 1;
 #pragma unroll
         for (int comp = 0; comp < 2; ++comp) {
             float F1, F2, F3, S1, S3 = 0.f;
@@ -567,29 +622,26 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             }
             (void)lam0;
             float* bpx = a.bp[side == 3 ? bpx0 + 2 * comp : bpx0 + comp];
-            const float Px = bpx[ap];
+            const float Px = gPx[comp];
             const float Pxn = ((1.0f - 0.5f * yx) * Px - dxc.dtdp * S1) * dxc.rh;
             bpx[ap] = Pxn;
-            float* b1 = a.bu[base + 3 * comp + 0][plane];
             float* b1n = a.bu[base + 3 * comp + 0][nplane];
-            float* b2 = a.bu[base + 3 * comp + 1][plane];
             float* b2n = a.bu[base + 3 * comp + 1][nplane];
-            float* b3 = a.bu[base + 3 * comp + 2][plane];
             float* b3n = a.bu[base + 3 * comp + 2][nplane];
-            const float u1 = b1[ap], u1m = b1n[ap];
+            const float u1 = gU1[comp], u1m = gU1m[comp];
             const float f1 = kd * (F1 + 0.5f * (Pxn + Px));
             float n1;
             if (side == 2 && iz != 1)
                 n1 = ((2.0f - yx * yx) * u1 - (1.0f - yx) * u1m) * dxc.r1 + f1;
             else
                 n1 = ((2.0f - yx * yx) * u1 - (1.0f - yx) * u1m + f1) * dxc.r1;
-            const float u2 = b2[ap], u2m = b2n[ap];
+            const float u2 = gU2[comp], u2m = gU2m[comp];
             const float n2 = ((2.0f - yx * yz) * u2 - (1.0f - 0.5f * (yx + yz)) * u2m + kd * F2) * r2;
-            const float u3 = b3[ap], u3m = b3n[ap];
+            const float u3 = gU3[comp], u3m = gU3m[comp];
             float n3;
             if (side == 3) {
                 float* bpz = a.bp[9 + 2 * comp];
-                const float Pz = bpz[ap];
+                const float Pz = gPz[comp];
                 const float Pzn = ((1.0f - 0.5f * yz) * Pz - dzc.dtdp * S3) * dzc.rh;
                 bpz[ap] = Pzn;
                 n3 = ((2.0f - yz * yz) * u3 - (1.0f - yz) * u3m + kd * (F3 + 0.5f * (Pzn + Pz))) * dzc.r1;

@@ -56,6 +56,9 @@ struct StepArgs {
     // displacement planes [level parity]
     float* ux[2];
     float* uz[2];
+    // frame of the fast path (u^n + outer background outside the regular domain), same layout
+    float* fux;
+    float* fuz;
     // PML split fields bu[array][plane] (24 arrays in updatedispl_ order; top unused)
     float* bu[24][2];
     float* bp[12];
@@ -116,11 +119,25 @@ struct BatchTab {
     int* live;                // [n] member takes part in the current step
     const int* edge_off;      // [n+1] first tiled-kernel block of each member
     const int* march_off;     // [n+1] first fast-path block of each member
+    const int* frame_off;     // [n+1] first frame block of each member
 };
 
 cudaError_t launch_step_batch(const BatchTab& t, int norder, int blocks, size_t smem, cudaStream_t s);
 cudaError_t launch_batch_bump(const BatchTab& t, cudaStream_t s);
-cudaError_t launch_march_batch(const BatchTab& t, int norder, int blocks, cudaStream_t s);
+// Frame (frame_blocks blocks) and fast path (blocks blocks) of a batch step.
+cudaError_t launch_march_batch(const BatchTab& t, int norder, int frame_blocks, int blocks, cudaStream_t s);
+// Blocks of one solve's frame launch (the kernel that writes StepArgs::fux / fuz before the fast path).
+int frame_blocks(const StepArgs& a);
+
+// Leading dimension of the planar arrays: NZ rows, or more when the fast path runs, whose last
+// 64-row band may reach past NZ (nz + 63 - 2*norder rows); the extra rows are padding (u = 0,
+// lambda = 0, mu = 1, dt^2/rho = 0), rounded to 32 rows.
+inline int plane_ldz(int nz, int npml, int norder, bool fast_path)
+{
+    int need = nz + npml;
+    if (fast_path && nz + 64 - 2 * norder > need) need = nz + 64 - 2 * norder;
+    return (need + 31) / 32 * 32;
+}
 
 constexpr int kMarchSeg = 64;
 constexpr int kMarchMaxOrder = 4;
