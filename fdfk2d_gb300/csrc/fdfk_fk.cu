@@ -12,8 +12,9 @@
 //      every layer's amplitudes (phase referenced at the layer top);
 //   4. fk_depth_response: U_R, U_Z per (model, grid row, frequency);
 //   5. fk_column_phase: W_k times the horizontal phase per (column, frequency);
-//   6. per batch of strip series: fk_assemble writes the half spectra,
-//      a batched Z2D inverse FFT (cuFFT) makes the real series, and
+//   6. per batch of strip series: fk_assemble folds each half spectrum into
+//      the input of a half-length complex inverse FFT (batched Z2Z, cuFFT,
+//      in place) whose output is the real series, and
 //      fk_epilogue scales by exp(alpha t)/N and transposes into the strips
 //      (time slowest), float32.
 #include "fdfk_fk.cuh"
@@ -310,25 +311,53 @@ __global__ void fk_column_phase(FkGeom g, int ncol, const double* __restrict__ D
 }
 
 // Half spectra of series [g0, g0 + nb): spec[b * (nh + 1) + k].
+// Bin j (0..nh) of the half spectrum of series p: W_j * phase * U (times cos(baz) for the x
+// component), zero from j = K on.
+__device__ __forceinline__ cd series_bin(const FkGeom& g, const SeriesTab& tab, const SeriesPos& p, int j,
+                                         const cd* __restrict__ U, const cd* __restrict__ Ph,
+                                         const double* __restrict__ cosphi)
+{
+    if (j >= g.K) return mk(0.0, 0.0);
+    const int c = p.ix - (1 - tab.nbd);
+    const bool xcomp = (p.s & 1) == 0;
+    const cd u = U[(((size_t)p.model * tab.nrow + (p.iz - 1)) * g.K + j) * 2 + (xcomp ? 0 : 1)];
+    cd v = cmul(Ph[(size_t)c * g.K + j], u);
+    if (xcomp) {
+        const double cp = cosphi[c];
+        v = mk(v.x * cp, v.y * cp);
+    }
+    return v;
+}
+
+// Input of the half-length complex inverse transform that yields a batch of real series: with
+// M = N/2 and X the half spectrum (X_0 and X_M enter with their real parts, as for a real series),
+//   Z_k = E_k + i O_k,  E_k = X_k + conj(X_{M-k}),  O_k = (X_k - conj(X_{M-k})) exp(+2 pi i k / N),
+// sum_k Z_k exp(+2 pi i k m / M) = x[2m] + i x[2m+1], x the length-N real inverse transform of X.
+// The complex output read as doubles is therefore x itself.
 __global__ void fk_assemble(FkGeom g, SeriesTab tab, long long g0, int nb, const cd* __restrict__ U,
-                            const cd* __restrict__ Ph, const double* __restrict__ cosphi, cd* __restrict__ spec)
+                            const cd* __restrict__ Ph, const double* __restrict__ cosphi, const cd* __restrict__ tw,
+                            cd* __restrict__ spec)
 {
     const int b = blockIdx.y;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nb || k > g.nh) return;
-    cd v = mk(0.0, 0.0);
-    if (k < g.K) {
+    const int M = g.nh;
+    if (b >= nb || k >= M) return;
+    cd z = mk(0.0, 0.0);
+    if (k < g.K || M - k < g.K) {
         const SeriesPos p = decode(tab, g0 + b);
-        const int c = p.ix - (1 - tab.nbd);
-        const bool xcomp = (p.s & 1) == 0;
-        const cd u = U[(((size_t)p.model * tab.nrow + (p.iz - 1)) * g.K + k) * 2 + (xcomp ? 0 : 1)];
-        v = cmul(Ph[(size_t)c * g.K + k], u);
-        if (xcomp) {
-            const double cp = cosphi[c];
-            v = mk(v.x * cp, v.y * cp);
+        cd xk = series_bin(g, tab, p, k, U, Ph, cosphi);
+        cd xm = series_bin(g, tab, p, M - k, U, Ph, cosphi);
+        if (k == 0) {
+            xk.y = 0.0;
+            xm.y = 0.0;
         }
+        const cd e = mk(xk.x + xm.x, xk.y - xm.y);
+        const cd d = mk(xk.x - xm.x, xk.y + xm.y);
+        const cd t = tw[k];                                 // exp(-2 pi i k / N)
+        const cd o = mk(d.x * t.x + d.y * t.y, d.y * t.x - d.x * t.y);   // d * conj(t)
+        z = mk(e.x - o.y, e.y + o.x);
     }
-    spec[(size_t)b * (g.nh + 1) + k] = v;
+    spec[(size_t)b * M + k] = z;
 }
 
 // strips[s][q + per_s * n] = float(y[b][n] * escale[n]), n = 0..nt; 32 x 32 tiles through shared memory.
@@ -469,34 +498,34 @@ struct DevBufs {
     }
 };
 
-// Batched Z2D plans, one per (device, length, batch), kept for the life of the process.  They
-// own no work area: each call supplies its own (stream-ordered), so calls on different streams
-// may use one plan at the same time.
-struct Z2DPlan {
+// Batched half-length Z2Z inverse plans, one per (device, length, batch), kept for the life of
+// the process.  They own no work area: each call supplies its own (stream-ordered), so calls on
+// different streams may use one plan at the same time.
+struct Z2ZPlan {
     cufftHandle h = 0;
     size_t work = 0;
 };
 
 std::mutex g_plan_mu;
-std::map<std::tuple<int, int, int>, Z2DPlan> g_plans;
+std::map<std::tuple<int, int, int>, Z2ZPlan> g_plans;
 
-cufftResult z2d_plan(int n, int batch, Z2DPlan& out)
+cufftResult z2z_plan(int m, int batch, Z2ZPlan& out)
 {
     int dev = 0;
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lock(g_plan_mu);
-    const auto key = std::make_tuple(dev, n, batch);
+    const auto key = std::make_tuple(dev, m, batch);
     auto it = g_plans.find(key);
     if (it != g_plans.end()) {
         out = it->second;
         return CUFFT_SUCCESS;
     }
-    Z2DPlan p;
+    Z2ZPlan p;
     cufftResult r = cufftCreate(&p.h);
     if (r != CUFFT_SUCCESS) return r;
-    int nn = n, inembed = n / 2 + 1, onembed = n;
+    int nn = m;
     if ((r = cufftSetAutoAllocation(p.h, 0)) != CUFFT_SUCCESS ||
-        (r = cufftMakePlanMany(p.h, 1, &nn, &inembed, 1, n / 2 + 1, &onembed, 1, n, CUFFT_Z2D, batch, &p.work)) !=
+        (r = cufftMakePlanMany(p.h, 1, &nn, nullptr, 1, m, nullptr, 1, m, CUFFT_Z2Z, batch, &p.work)) !=
             CUFFT_SUCCESS) {
         cufftDestroy(p.h);
         return r;
@@ -642,7 +671,7 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
 
     DevBufs B(stream);
     FkLayer *d_lay0, *d_lay1;
-    double *d_w, *d_esc, *d_cos, *d_D, *d_y;
+    double *d_w, *d_esc, *d_cos, *d_D;
     cd *d_tw, *d_W, *d_amp0, *d_amp1, *d_U, *d_Ph, *d_spec;
     FK_CK(B.alloc(&d_lay0, lay[0].size()));
     FK_CK(B.alloc(&d_lay1, lay[1].size()));
@@ -682,8 +711,8 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
     nl += 5;
     FK_CK(cudaGetLastError());
 
-    // batches of series: half spectrum (nh + 1 complex) and real series (N) per series
-    const size_t per_series = (size_t)(g.nh + 1) * sizeof(cd) + (size_t)g.N * sizeof(double);
+    // batches of series: the half-length complex transform runs in place, N doubles per series
+    const size_t per_series = (size_t)g.N * sizeof(double);
     const size_t budget = (size_t)2 << 30;
     long long bmax = std::max<long long>(1, std::min<long long>(nseries, (long long)(budget / per_series)));
     if (const char* e = std::getenv("FDFK_FK_BATCH")) {   // series per batch (tuning and tests)
@@ -691,24 +720,24 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
         if (v > 0) bmax = std::min(bmax, v);
     }
     const int nb_full = (int)std::min<long long>(bmax, 65535);
-    FK_CK(B.alloc(&d_spec, (size_t)nb_full * (g.nh + 1)));
-    FK_CK(B.alloc(&d_y, (size_t)nb_full * g.N));
+    FK_CK(B.alloc(&d_spec, (size_t)nb_full * g.nh));
     const int tail = (int)(nseries % nb_full);
-    Z2DPlan plan_full, plan_tail;
-    FFT_CK(z2d_plan(g.N, nb_full, plan_full));
-    if (tail && nseries > nb_full) FFT_CK(z2d_plan(g.N, tail, plan_tail));
+    Z2ZPlan plan_full, plan_tail;
+    FFT_CK(z2z_plan(g.nh, nb_full, plan_full));
+    if (tail && nseries > nb_full) FFT_CK(z2z_plan(g.nh, tail, plan_tail));
     void* work = nullptr;
     FK_CK(B.alloc(reinterpret_cast<char**>(&work), std::max(plan_full.work, plan_tail.work)));
     for (long long g0 = 0; g0 < nseries; g0 += nb_full) {
         const int nb = (int)std::min<long long>(nb_full, nseries - g0);
-        const dim3 ga((g.nh + 1 + 255) / 256, nb);
-        fk_assemble<<<ga, 256, 0, stream>>>(g, tab, g0, nb, d_U, d_Ph, d_cos, d_spec);
-        const Z2DPlan& pl = nb == nb_full ? plan_full : plan_tail;
+        const dim3 ga((g.nh + 255) / 256, nb);
+        fk_assemble<<<ga, 256, 0, stream>>>(g, tab, g0, nb, d_U, d_Ph, d_cos, d_tw, d_spec);
+        const Z2ZPlan& pl = nb == nb_full ? plan_full : plan_tail;
         FFT_CK(cufftSetWorkArea(pl.h, work));
         FFT_CK(cufftSetStream(pl.h, stream));
-        FFT_CK(cufftExecZ2D(pl.h, (cufftDoubleComplex*)d_spec, d_y));
+        FFT_CK(cufftExecZ2Z(pl.h, (cufftDoubleComplex*)d_spec, (cufftDoubleComplex*)d_spec, CUFFT_INVERSE));
         const dim3 ge((J.nt + 1 + 31) / 32, (nb + 31) / 32);
-        fk_epilogue<<<ge, dim3(32, 8), 0, stream>>>(tab, g0, nb, g.N, J.nt, d_y, d_esc);
+        fk_epilogue<<<ge, dim3(32, 8), 0, stream>>>(tab, g0, nb, g.N, J.nt, reinterpret_cast<const double*>(d_spec),
+                                                    d_esc);
         nl += 2;
         FK_CK(cudaGetLastError());
     }
