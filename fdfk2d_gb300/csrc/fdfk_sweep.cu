@@ -66,6 +66,22 @@ __device__ __forceinline__ float fast_rcp(float x)
     return r;
 }
 
+// (i % n, i / n) along i = i0, i0 + step, ... without a division per step.
+struct Walk {
+    int r, q, dr, dq, n;
+    __device__ __forceinline__ Walk(int i0, int n_, int step)
+        : r(i0 % n_), q(i0 / n_), dr(step % n_), dq(step / n_), n(n_) {}
+    __device__ __forceinline__ void next()
+    {
+        r += dr;
+        q += dq;
+        if (r >= n) {
+            r -= n;
+            ++q;
+        }
+    }
+};
+
 __device__ __forceinline__ int ordx(const StepArgs& a, int ix, int NO)
 {
     int n = min(min(ix + a.npml - 1, a.nx + a.npml - ix), NO);
@@ -321,8 +337,9 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
 #define SM(arr, z, x) arr[((x) + NO) * T.MZ + ((z) + NO)]
 
     // ---- phase 1a: x-direction staggered products and dzx operands -----------
-    for (int i = tid; i < T.AX; i += kThreads) {
-        int z = i % TZ, xl = i / TZ;
+    Walk w1(tid, TZ, kThreads);
+    for (int i = tid; i < T.AX; i += kThreads, w1.next()) {
+        const int z = w1.r, xl = w1.q;
         int iz = R.z0 + z;
         // staggered product at label L = xl - NO (half point between L and L+1)
         if (xl < T.XW - 1) {
@@ -360,8 +377,9 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         }
     }
     // ---- phase 1b: z-direction staggered products and dxz operands -----------
-    for (int i = tid; i < T.AZ; i += kThreads) {
-        int zl = i % T.ZW, x = i / T.ZW;
+    Walk w2(tid, T.ZW, kThreads);
+    for (int i = tid; i < T.AZ; i += kThreads, w2.next()) {
+        const int zl = w2.r, x = w2.q;
         int ix = R.x0 + x;
         if (zl < T.ZW - 1) {
             int L = zl - NO;
@@ -406,8 +424,9 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
     // ---- phase 2: output cells ----------------------------------------------
     const float dx = a.dx, dz = a.dz;
     const float dx2 = pml ? a.dx2p : a.dx2r;
-    for (int cell = tid; cell < TZ * TX; cell += kThreads) {
-        const int z = cell % TZ, x = cell / TZ;
+    Walk wc(tid, TZ, kThreads);
+    for (int cell = tid; cell < TZ * TX; cell += kThreads, wc.next()) {
+        const int z = wc.r, x = wc.q;
         const int iz = R.z0 + z;
         const int ix = R.x0 + x;
         if (iz < R.zlo || iz > R.zhi || ix < R.xlo || ix > R.xhi) continue;
@@ -683,7 +702,7 @@ __device__ __forceinline__ int batch_member(const int* __restrict__ off, int n, 
 
 // The tiled kernel over every member of a batch: member s owns blocks edge_off[s] .. edge_off[s+1]-1.
 template <int NO>
-__global__ void __launch_bounds__(kThreads, 4) fdfk_step_batch_kernel(BatchTab t)
+__global__ void __launch_bounds__(kThreads, 3) fdfk_step_batch_kernel(BatchTab t)
 {
     const int s = batch_member(t.edge_off, t.n, blockIdx.x);
     if (!t.live[s]) return;
