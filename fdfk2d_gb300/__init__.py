@@ -23,10 +23,12 @@ There is no CPU fallback: if the CUDA library is missing or no GPU is
 visible, calls raise.
 """
 from .api import (Batch, FDFKError, FkParams, Params, Server, Session, autotune, backazimuths, read_input, read_su, run,
+                  receiver_functions,
                   session_device_bytes, stable_dt, write_su, STRIPS, BP, BU, comput_background_wavefield,
                   fk_background, lib, lib_path, simulate, strip_shapes, pml_shapes, updatedispl, kernel_launches)
 
-__all__ = ["Batch", "FDFKError", "Server", "autotune", "backazimuths", "read_input", "read_su", "run", "session_device_bytes",
+__all__ = ["Batch", "FDFKError", "Server", "autotune", "backazimuths", "read_input", "read_su", "receiver_functions", "run",
+           "session_device_bytes",
            "stable_dt", "write_su", "FkParams", "Params", "Session", "STRIPS", "BP", "BU", "comput_background_wavefield",
            "fk_background", "lib", "lib_path", "simulate", "strip_shapes", "pml_shapes", "updatedispl",
            "kernel_launches"]

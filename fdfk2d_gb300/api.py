@@ -118,7 +118,7 @@ def lib():
                      "fdfk_server_create", "fdfk_server_submit", "fdfk_server_pump", "fdfk_server_request",
                      "fdfk_server_get_stats", "fdfk_input_read", "fdfk_backazimuths", "fdfk_stable_dt",
                      "fdfk_write_su", "fdfk_run", "fdfk_session_snapshot", "fdfk_session_set_tuning",
-                     "fdfk_session_get_tuning", "fdfk_autotune"):
+                     "fdfk_session_get_tuning", "fdfk_autotune", "fdfk_rf_itdecon"):
             getattr(L, name).restype = C.c_int if name != "fdfk_session_destroy" else None
         _lib = L
     return _lib
@@ -463,6 +463,37 @@ def autotune(p: dict, c, steps: int = 20):
     a, b, ms = C.c_int(), C.c_int(), C.c_float()
     _check(lib().fdfk_autotune(C.byref(prm), _f32(c, "c"), C.c_int(int(steps)), C.byref(a), C.byref(b), C.byref(ms)))
     return a.value, b.value, ms.value
+
+
+def receiver_functions(num, den, dt: float, minlag: float, maxlag: float, tshift: float = 0.0, f0: float = 8.0,
+                       itmax: int = 100, minderr: float = 1e-3):
+    """Receiver functions by iterative time-domain deconvolution, one per trace (fdfk_rf_itdecon; the
+    computation of utils/makeRFitdecon.m, FP64 on the GPU).  num, den: (nt,) or (nt, ntr) traces, e.g. the
+    radial and vertical seismograms of a solve for P-to-S.  Returns (rf (nrf, ntr), rms list of per-iteration
+    misfits per trace, iterations per trace); 1-D inputs give a 1-D rf and a single rms array."""
+    a = np.asarray(num, np.float32)
+    b = np.asarray(den, np.float32)
+    one = a.ndim == 1
+    a = np.asfortranarray(a.reshape(a.shape[0], -1))
+    b = np.asfortranarray(b.reshape(b.shape[0], -1))
+    if a.shape != b.shape:
+        raise ValueError("numerator and denominator shapes differ")
+    nt, ntr = a.shape
+    nrf = C.c_int()
+    args = (C.c_int(nt), C.c_int(ntr), C.c_int(nt), C.c_double(dt), C.c_double(minlag), C.c_double(maxlag),
+            C.c_double(tshift), C.c_double(f0), C.c_int(itmax), C.c_double(minderr))
+    _check(lib().fdfk_rf_itdecon(a.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p), *args, None,
+                                 C.c_int(0), C.byref(nrf), None, None))
+    rf = np.zeros((nrf.value, ntr), np.float64, order="F")
+    rms = np.zeros((max(itmax, 1), ntr), np.float64, order="F")
+    its = np.zeros(ntr, np.int32)
+    _check(lib().fdfk_rf_itdecon(a.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p), *args,
+                                 rf.ctypes.data_as(C.c_void_p), C.c_int(max(nrf.value, 1)), C.byref(nrf),
+                                 rms.ctypes.data_as(C.c_void_p), its.ctypes.data_as(C.c_void_p)))
+    rmsl = [rms[:its[j], j].copy() for j in range(ntr)]
+    if one:
+        return rf[:, 0], rmsl[0], int(its[0])
+    return rf, rmsl, its
 
 
 def backazimuths(lat_org, lon_org, az_org, evla, evlo, coordx) -> np.ndarray:

@@ -16,7 +16,8 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libfdfk_gb300.so")
-SOURCES = ("fdfk_sweep.cu", "fdfk_capi.cu", "fdfk_fk.cu", "fdfk_noalloc.cu", "fdfk_batch.cu", "fdfk_server.cu", "fdfk_io.cpp")
+SOURCES = ("fdfk_sweep.cu", "fdfk_capi.cu", "fdfk_fk.cu", "fdfk_noalloc.cu", "fdfk_batch.cu", "fdfk_server.cu", "fdfk_io.cpp",
+           "fdfk_rf.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -154,6 +154,26 @@ int fdfk_session_snapshot(fdfk_session* s, float* ux, float* uz);
 void fdfk_session_destroy(fdfk_session* s);
 
 /*
+ * Receiver functions by iterative time-domain deconvolution, one per trace:
+ * the computation of utils/makeRFitdecon.m (called from utils/plot_PRF.m and
+ * plot_SRF.m on a solve's seismograms), in FP64 on the GPU, one block per
+ * trace.  num (radial for P-to-S) and den (vertical) hold ntr traces of nt
+ * samples, trace j at num + j*ld; dt in s; minlag, maxlag, tshift in s (the
+ * reference halves minlag / maxlag until the lags fit the trace); f0 the
+ * Gaussian width; at most itmax (<= 4096) spikes while the misfit improves by
+ * more than minderr (percent).  Writes *nrf, the receiver-function length
+ * (it depends only on the lags and tshift); with rf == NULL nothing else is
+ * done.  Otherwise rf receives trace j's receiver function at rf + j*ldrf
+ * (ldrf >= *nrf), rms the misfit after each iteration at rms + j*itmax and
+ * iters the iterations done.  Replaces the MATLAB function
+ * makeRFitdecon(UIN, WIN, DT, MINLAG, MAXLAG, TSHIFT, F0, ITMAX, MINDERR, 0)
+ * (utils/makeRFitdecon.m:1-3).
+ */
+int fdfk_rf_itdecon(const float* num, const float* den, int nt, int ntr, int ld, double dt, double minlag,
+                    double maxlag, double tshift, double f0, int itmax, double minderr, double* rf, int ldrf,
+                    int* nrf, double* rms, int* iters);
+
+/*
  * The input folder of FDFK2D (src/Input.f90): the inpar file names, in
  * order, the FD model, source, receiver, left and right FK model, Vp and Vs
  * model files.  Text files are read with Fortran list-directed rules; the
