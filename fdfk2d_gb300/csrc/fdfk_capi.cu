@@ -145,27 +145,29 @@ void free_session(fdfk_session* s)
     delete s;
 }
 
+// Material planes from c(3, NZ, NX): the raw array is copied to the device (stream-ordered
+// scratch) and converted there (launch_material), then the validity flags are read back.
 int upload_material(fdfk_session* s, const float* c)
 {
-    const fdfk_params& p = s->p;
-    const size_t n = (size_t)s->ldz * s->NX;
-    std::vector<float> k(n, 0.f), l(n, 0.f), m(n, 1.f);
-    const double dt2 = p.dt * p.dt;
-    for (int x = 0; x < s->NX; ++x)
-        for (int z = 0; z < s->NZ; ++z) {
-            size_t src = 3 * ((size_t)z + (size_t)s->NZ * x);
-            size_t dst = (size_t)z + (size_t)s->ldz * x;
-            if (!(c[src] > 0.f)) return fail(FDFK_EINVAL, "density must be positive everywhere");
-            k[dst] = (float)(dt2 / (double)c[src]);
-            l[dst] = c[src + 1];
-            m[dst] = c[src + 2];
-            if (!(m[dst] > 0.f) || !(l[dst] + 2.0f * m[dst] > 0.f))
-                return fail(FDFK_EINVAL, "mu and lambda+2mu must be positive everywhere");
-        }
-    CK(cudaMemcpyAsync(s->kdt2, k.data(), n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    CK(cudaMemcpyAsync(s->lam, l.data(), n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    CK(cudaMemcpyAsync(s->mu, m.data(), n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
+    const size_t nc = 3 * (size_t)s->NZ * s->NX;
+    float* d_c = nullptr;
+    int* d_flag = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&d_c, nc * sizeof(float), s->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_flag, sizeof(int), s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_flag, 0, sizeof(int), s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_c, c, nc * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess)
+        e = launch_material(d_c, s->NZ, s->NX, s->ldz, s->p.dt * s->p.dt, s->kdt2, s->lam, s->mu, d_flag, s->stream);
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
+    if (d_c) cudaFreeAsync(d_c, s->stream);
+    if (d_flag) cudaFreeAsync(d_flag, s->stream);
+    const cudaError_t e2 = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("material upload: ") + cudaGetErrorString(e));
+    g_launches += 1;
+    if (flag & 1) return fail(FDFK_EINVAL, "density must be positive everywhere");
+    if (flag & 2) return fail(FDFK_EINVAL, "mu and lambda+2mu must be positive everywhere");
     return FDFK_OK;
 }
 

@@ -146,6 +146,14 @@ __global__ void na_pack_bu(DeintTab t, int npml, int NX)
         }                                                                                        \
     } while (0)
 
+cudaError_t launch_material(const float* c, int NZ, int NX, int ldz, double dt2, float* kd, float* la, float* mu,
+                            int* flag, cudaStream_t st)
+{
+    const long long n = (long long)ldz * NX;
+    na_material<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(c, NZ, NX, ldz, dt2, kd, la, mu, flag);
+    return cudaGetLastError();
+}
+
 size_t noalloc_floats_needed(const fdfk_params& p)
 {
     const size_t NZ = p.nz + p.npml, NX = p.nx + 2 * p.npml, ldz = (NZ + 31) / 32 * 32, n = ldz * NX;
@@ -273,7 +281,7 @@ int step_noalloc(const fdfk_params& p, int it, const float* const strips[12], co
     NA_CK(cudaMemsetAsync(flag, 0, sizeof(int), st));   // the status flag must start at zero
 
     const unsigned nb = (unsigned)((n + 255) / 256);
-    na_material<<<nb, 256, 0, st>>>(rc, NZ, NX, ldz, p.dt * p.dt, kd, la, mu, flag);
+    NA_CK(launch_material(rc, NZ, NX, ldz, p.dt * p.dt, kd, la, mu, flag, st));
     na_unpack_u<<<nb, 256, 0, st>>>(rux, ruz, NZ, NX, ldz, ux0, ux1, uz0, uz1);
     const dim3 gb((unsigned)std::min<long long>((mmax + 255) / 256, 1024), 18);
     na_unpack_bu<<<gb, 256, 0, st>>>(tab);
