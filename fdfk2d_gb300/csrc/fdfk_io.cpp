@@ -177,7 +177,7 @@ double backaz(double evla, double evlo, double stla, double stlo)
     const double scola = 0.5 * kPi - std::atan(coeff * std::tan(stla * kDeg2Rad));
     const double ecola = 0.5 * kPi - std::atan(coeff * std::tan(evla * kDeg2Rad));
     const double slon = stlo * kDeg2Rad, elon = evlo * kDeg2Rad;
-    const double a = std::sin(scola) * std::cos(slon), b = std::sin(scola) * std::sin(slon), c = std::cos(scola);
+    const double c = std::cos(scola);
     const double d = std::sin(slon), e = -std::cos(slon);
     const double g = -c * e, h = c * d, k = -std::sin(scola);
     const double aa = std::sin(ecola) * std::cos(elon), bb = std::sin(ecola) * std::sin(elon), cc = std::cos(ecola);

@@ -91,21 +91,6 @@ __device__ __forceinline__ void dz_coll(float a0, float a1, float& d0, float& d1
     d1 = s1;
 }
 
-// sum_j c0_j (q(L+j) - q(L+1-j)) at the half rows L = r0, r0+1 (label = upper row)
-template <int NO>
-__device__ __forceinline__ void dz_stag(float a0, float a1, float& d0, float& d1)
-{
-    const ZCol<1 - NO, NO + 1> z(a0, a1);
-    float s0 = 0.f, s1 = 0.f;
-#pragma unroll
-    for (int j = 1; j <= NO; ++j) {
-        s0 = fmaf(c_stag[NO][j], z(j) - z(1 - j), s0);
-        s1 = fmaf(c_stag[NO][j], z(j + 1) - z(2 - j), s1);
-    }
-    d0 = s0;
-    d1 = s1;
-}
-
 // sum_k c0_k (G(r+k-1) - G(r-k)) of half-row quantities G at this lane's rows
 template <int NO>
 __device__ __forceinline__ void dz_half(float g0, float g1, float& d0, float& d1)
