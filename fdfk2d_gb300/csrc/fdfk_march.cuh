@@ -184,9 +184,11 @@ __global__ void __launch_bounds__(kFrameThreads) fdfk_frame_kernel(StepArgs a)
 // The frames of every live member of a batch: member s owns blocks frame_off[s] .. frame_off[s+1]-1.
 __global__ void __launch_bounds__(kFrameThreads) fdfk_frame_batch_kernel(BatchTab t)
 {
+    __shared__ StepArgs sa;
     const int s = batch_member(t.frame_off, t.n, blockIdx.x);
     if (!t.live[s]) return;
-    frame_cell(t.args[s], (long long)(blockIdx.x - t.frame_off[s]) * kFrameThreads + threadIdx.x);
+    stage_args(sa, t.args + s);
+    frame_cell(sa, (long long)(blockIdx.x - t.frame_off[s]) * kFrameThreads + threadIdx.x);
 }
 
 // Blocks of one member's frame launch.
@@ -205,9 +207,11 @@ __global__ void __launch_bounds__(128) fdfk_march_kernel(StepArgs a, MarchArgs m
 template <int NO>
 __global__ void __launch_bounds__(128) fdfk_march_batch_kernel(BatchTab t)
 {
+    __shared__ StepArgs sa;
     const int s = batch_member(t.march_off, t.n, blockIdx.x);
     if (!t.live[s]) return;
-    march_warp<NO>(t.args[s], t.march[s], (blockIdx.x - t.march_off[s]) * (blockDim.x >> 5) + (threadIdx.x >> 5));
+    stage_args(sa, t.args + s);
+    march_warp<NO>(sa, t.march[s], (blockIdx.x - t.march_off[s]) * (blockDim.x >> 5) + (threadIdx.x >> 5));
 }
 
 template <int NO>

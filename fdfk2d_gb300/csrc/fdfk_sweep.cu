@@ -688,6 +688,18 @@ __global__ void __launch_bounds__(kThreads, 3) fdfk_step_kernel(StepArgs a)
     step_block<NO>(a, blockIdx.x);
 }
 
+// A batch member's StepArgs copied by the whole block into shared memory (one barrier): the
+// batched kernels then read their arguments from there instead of global memory throughout
+// (the single-solve kernels have them as kernel parameters).
+__device__ __forceinline__ void stage_args(StepArgs& dst, const StepArgs* src)
+{
+    static_assert(sizeof(StepArgs) % sizeof(int) == 0, "StepArgs is copied as words");
+    const int* from = reinterpret_cast<const int*>(src);
+    int* to = reinterpret_cast<int*>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(StepArgs) / sizeof(int)); i += blockDim.x) to[i] = __ldg(from + i);
+    __syncthreads();
+}
+
 // Largest s with off[s] <= blk (off[0] = 0, off[n] = total blocks).
 __device__ __forceinline__ int batch_member(const int* __restrict__ off, int n, int blk)
 {
@@ -704,9 +716,11 @@ __device__ __forceinline__ int batch_member(const int* __restrict__ off, int n, 
 template <int NO>
 __global__ void __launch_bounds__(kThreads, 3) fdfk_step_batch_kernel(BatchTab t)
 {
+    __shared__ StepArgs sa;
     const int s = batch_member(t.edge_off, t.n, blockIdx.x);
-    if (!t.live[s]) return;
-    step_block<NO>(t.args[s], blockIdx.x - t.edge_off[s]);
+    if (!t.live[s]) return;                // the whole block returns: no barrier is split
+    stage_args(sa, t.args + s);
+    step_block<NO>(sa, blockIdx.x - t.edge_off[s]);
 }
 
 // Per-step bookkeeping of a batch on the device: time index, plane parity and receiver sampling of
