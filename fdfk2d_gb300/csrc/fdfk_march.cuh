@@ -48,6 +48,15 @@ __device__ __forceinline__ float frcp(float x)
     return r;
 }
 
+// c * a + b on both rows of a lane at once (one packed FFMA2; per row the same rounding as fmaf).
+__device__ __forceinline__ float2 ffma2(float c, float2 a, float2 b) { return __ffma2_rn(make_float2(c, c), a, b); }
+__device__ __forceinline__ float2 ffma2(float2 c, float2 a, float2 b) { return __ffma2_rn(c, a, b); }
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fmul2(float c, float2 a) { return __fmul2_rn(make_float2(c, c), a); }
+__device__ __forceinline__ float2 fmul2(float2 a, float c) { return __fmul2_rn(a, make_float2(c, c)); }
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 frcp2(float2 x) { return make_float2(frcp(x.x), frcp(x.y)); }
+
 // Value of a two-rows-per-lane quantity at row offset D from this lane's first row.
 template <int D>
 __device__ __forceinline__ float zrow(float a0, float a1)
@@ -81,14 +90,11 @@ template <int NO>
 __device__ __forceinline__ void dz_coll(float a0, float a1, float& d0, float& d1)
 {
     const ZCol<-NO, NO + 1> z(a0, a1);
-    float s0 = 0.f, s1 = 0.f;
+    float2 s = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int k = 1; k <= NO; ++k) {
-        s0 = fmaf(c_coll[NO][k], z(k) - z(-k), s0);
-        s1 = fmaf(c_coll[NO][k], z(k + 1) - z(1 - k), s1);
-    }
-    d0 = s0;
-    d1 = s1;
+    for (int k = 1; k <= NO; ++k) s = ffma2(c_coll[NO][k], make_float2(z(k) - z(-k), z(k + 1) - z(1 - k)), s);
+    d0 = s.x;
+    d1 = s.y;
 }
 
 // sum_k c0_k (G(r+k-1) - G(r-k)) of half-row quantities G at this lane's rows
@@ -96,14 +102,11 @@ template <int NO>
 __device__ __forceinline__ void dz_half(float g0, float g1, float& d0, float& d1)
 {
     const ZCol<-NO, NO> z(g0, g1);
-    float s0 = 0.f, s1 = 0.f;
+    float2 s = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int k = 1; k <= NO; ++k) {
-        s0 = fmaf(c_stag[NO][k], z(k - 1) - z(-k), s0);
-        s1 = fmaf(c_stag[NO][k], z(k) - z(1 - k), s1);
-    }
-    d0 = s0;
-    d1 = s1;
+    for (int k = 1; k <= NO; ++k) s = ffma2(c_stag[NO][k], make_float2(z(k - 1) - z(-k), z(k) - z(1 - k)), s);
+    d0 = s.x;
+    d1 = s.y;
 }
 
 }  // namespace march

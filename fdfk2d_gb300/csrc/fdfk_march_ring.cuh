@@ -53,26 +53,20 @@ __device__ __forceinline__ void cp_async4_s(unsigned s, const float* g)
 template <int NO>
 __device__ __forceinline__ void zc_stag(const ZCol<-NO, NO + 1>& z, float& d0, float& d1)
 {
-    float s0 = 0.f, s1 = 0.f;
+    float2 s = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int j = 1; j <= NO; ++j) {
-        s0 = fmaf(c_stag[NO][j], z(j) - z(1 - j), s0);
-        s1 = fmaf(c_stag[NO][j], z(j + 1) - z(2 - j), s1);
-    }
-    d0 = s0;
-    d1 = s1;
+    for (int j = 1; j <= NO; ++j) s = ffma2(c_stag[NO][j], make_float2(z(j) - z(1 - j), z(j + 1) - z(2 - j)), s);
+    d0 = s.x;
+    d1 = s.y;
 }
 template <int NO>
 __device__ __forceinline__ void zc_coll(const ZCol<-NO, NO + 1>& z, float& d0, float& d1)
 {
-    float s0 = 0.f, s1 = 0.f;
+    float2 s = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int k = 1; k <= NO; ++k) {
-        s0 = fmaf(c_coll[NO][k], z(k) - z(-k), s0);
-        s1 = fmaf(c_coll[NO][k], z(k + 1) - z(1 - k), s1);
-    }
-    d0 = s0;
-    d1 = s1;
+    for (int k = 1; k <= NO; ++k) s = ffma2(c_coll[NO][k], make_float2(z(k) - z(-k), z(k + 1) - z(1 - k)), s);
+    d0 = s.x;
+    d1 = s.y;
 }
 
 template <int NO>
@@ -155,23 +149,19 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
     for (int c = c0; c < m0 + RG::kAhead; ++c) issue(c);
     cp_wait<RG::kAhead>();                      // columns c0 .. m0-1 have landed
 
-    float SA[NS][2], SB[NS][2];
-    float D2[ND][2], D3[ND][2];
-    float FX[NF][2], FZ[NF][2];
+    float2 SA[NS], SB[NS], D2[ND], D3[ND], FX[NF], FZ[NF];
+    const float2 zero2 = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int i = 0; i < NS; ++i) SA[i][0] = SA[i][1] = SB[i][0] = SB[i][1] = 0.f;
+    for (int i = 0; i < NS; ++i) SA[i] = SB[i] = zero2;
 #pragma unroll
-    for (int i = 0; i < ND; ++i) D2[i][0] = D2[i][1] = D3[i][0] = D3[i][1] = 0.f;
+    for (int i = 0; i < ND; ++i) D2[i] = D3[i] = zero2;
 #pragma unroll
-    for (int i = 0; i < NF; ++i) FX[i][0] = FX[i][1] = FZ[i][0] = FZ[i][1] = 0.f;
+    for (int i = 0; i < NF; ++i) FX[i] = FZ[i] = zero2;
 
-    float lp0, lp1, mp0, mp1, rlp0, rlp1, rmp0, rmp1;
-    {
-        const float2 l = rdA(c0, 2), mm = rdA(c0, 3);
-        lp0 = l.x; lp1 = l.y; mp0 = mm.x; mp1 = mm.y;
-        rlp0 = frcp(lp0 + 2.0f * mp0); rlp1 = frcp(lp1 + 2.0f * mp1);
-        rmp0 = frcp(mp0); rmp1 = frcp(mp1);
-    }
+    // lambda + 2 mu is formed with one rounding (2 mu is exact), as by a fused multiply-add
+    const float2 two = make_float2(2.0f, 2.0f);
+    float2 LP = rdA(c0, 2), MP = rdA(c0, 3);
+    float2 RLP = frcp2(ffma2(two, MP, LP)), RMP = frcp2(MP);
 
     for (int mc = m0; mc <= m1; ++mc) {
         issue(mc + RG::kAhead);
@@ -179,44 +169,39 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
         const float2 U = rdA(mc, 0), Z = rdA(mc, 1), LNv = rdA(mc, 2), MNv = rdA(mc, 3);
         const float2 LQv = rdA(mc - NO + 1, 2), MQv = rdA(mc - NO + 1, 3);
         const float ux0 = U.x, ux1 = U.y, uz0 = Z.x, uz1 = Z.y;
-        const float ln0 = LNv.x, ln1 = LNv.y, mn0 = MNv.x, mn1 = MNv.y;
-        const float lq0 = LQv.x, lq1 = LQv.y, mq0 = MQv.x, mq1 = MQv.y;
         const int xc = mc - LAG;
         const bool emit = xc >= xs;
 
-        // --- x-staggered derivative
-        float sa0 = fmaf(c_stag[NO][NO], ux0, SA[0][0]), sa1 = fmaf(c_stag[NO][NO], ux1, SA[0][1]);
-        float sb0 = fmaf(c_stag[NO][NO], uz0, SB[0][0]), sb1 = fmaf(c_stag[NO][NO], uz1, SB[0][1]);
+        // --- x-staggered derivative (both rows of the lane in one packed FMA)
+        const float2 sa = ffma2(c_stag[NO][NO], U, SA[0]), sb = ffma2(c_stag[NO][NO], Z, SB[0]);
 #pragma unroll
         for (int i = 0; i < NS - 1; ++i) {
             const int ip = i + 1;
             const float c = ip < NO ? c_stag[NO][NO - ip] : -c_stag[NO][ip - NO + 1];
-            SA[i][0] = fmaf(c, ux0, SA[ip][0]); SA[i][1] = fmaf(c, ux1, SA[ip][1]);
-            SB[i][0] = fmaf(c, uz0, SB[ip][0]); SB[i][1] = fmaf(c, uz1, SB[ip][1]);
+            SA[i] = ffma2(c, U, SA[ip]);
+            SB[i] = ffma2(c, Z, SB[ip]);
         }
-        SA[NS - 1][0] = 0.f; SA[NS - 1][1] = 0.f; SB[NS - 1][0] = 0.f; SB[NS - 1][1] = 0.f;
+        SA[NS - 1] = SB[NS - 1] = zero2;
 
-        const float rlq0 = frcp(lq0 + 2.0f * mq0), rlq1 = frcp(lq1 + 2.0f * mq1);
-        const float rmq0 = frcp(mq0), rmq1 = frcp(mq1);
-        const float ga0 = 2.0f * frcp(rlp0 + rlq0) * sa0 * dx2, ga1 = 2.0f * frcp(rlp1 + rlq1) * sa1 * dx2;
-        const float gb0 = 2.0f * frcp(rmp0 + rmq0) * sb0 * dx2, gb1 = 2.0f * frcp(rmp1 + rmq1) * sb1 * dx2;
+        const float2 RLQ = frcp2(ffma2(two, MQv, LQv)), RMQ = frcp2(MQv);
+        const float2 ga = fmul2(fmul2(fmul2(two, frcp2(fadd2(RLP, RLQ))), sa), dx2);
+        const float2 gb = fmul2(fmul2(fmul2(two, frcp2(fadd2(RMP, RMQ))), sb), dx2);
 
         // --- x-collocated derivative
-        const float d20 = fmaf(c_coll[NO][NO], uz0, D2[0][0]), d21 = fmaf(c_coll[NO][NO], uz1, D2[0][1]);
-        const float d30 = fmaf(c_coll[NO][NO], ux0, D3[0][0]), d31 = fmaf(c_coll[NO][NO], ux1, D3[0][1]);
+        const float2 d2 = ffma2(c_coll[NO][NO], Z, D2[0]), d3 = ffma2(c_coll[NO][NO], U, D3[0]);
 #pragma unroll
         for (int j = 0; j < ND - 1; ++j) {
             const int jp = j + 1;
             if (jp == NO) {
-                D2[j][0] = D2[jp][0]; D2[j][1] = D2[jp][1];
-                D3[j][0] = D3[jp][0]; D3[j][1] = D3[jp][1];
+                D2[j] = D2[jp];
+                D3[j] = D3[jp];
             } else {
                 const float c = jp < NO ? c_coll[NO][NO - jp] : -c_coll[NO][jp - NO];
-                D2[j][0] = fmaf(c, uz0, D2[jp][0]); D2[j][1] = fmaf(c, uz1, D2[jp][1]);
-                D3[j][0] = fmaf(c, ux0, D3[jp][0]); D3[j][1] = fmaf(c, ux1, D3[jp][1]);
+                D2[j] = ffma2(c, Z, D2[jp]);
+                D3[j] = ffma2(c, U, D3[jp]);
             }
         }
-        D2[ND - 1][0] = 0.f; D2[ND - 1][1] = 0.f; D3[ND - 1][0] = 0.f; D3[ND - 1][1] = 0.f;
+        D2[ND - 1] = D3[ND - 1] = zero2;
 
         // --- z-direction terms of column mc (one shuffled column per field for every z-stencil)
         const ZCol<-NO, NO + 1> zz(uz0, uz1), zx(ux0, ux1);
@@ -225,75 +210,75 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
             float sza0, sza1, szb0, szb1;
             zc_stag<NO>(zz, sza0, sza1);
             zc_stag<NO>(zx, szb0, szb1);
-            const float rl0 = frcp(ln0 + 2.0f * mn0), rl1 = frcp(ln1 + 2.0f * mn1);
-            const float rm0 = frcp(mn0), rm1 = frcp(mn1);
-            const float rl2 = zrow<2>(rl0, rl1), rm2 = zrow<2>(rm0, rm1);
-            const float gzA0 = 2.0f * frcp(rl0 + rl1) * sza0, gzA1 = 2.0f * frcp(rl1 + rl2) * sza1;
-            const float gzB0 = 2.0f * frcp(rm0 + rm1) * szb0, gzB1 = 2.0f * frcp(rm1 + rm2) * szb1;
-            dz_half<NO>(gzA0, gzA1, z2a0, z2a1);
-            dz_half<NO>(gzB0, gzB1, z2b0, z2b1);
+            const float2 RL = frcp2(ffma2(two, MNv, LNv)), RM = frcp2(MNv);
+            const float rl2 = zrow<2>(RL.x, RL.y), rm2 = zrow<2>(RM.x, RM.y);
+            const float2 gzA = fmul2(fmul2(two, frcp2(fadd2(RL, make_float2(RL.y, rl2)))), make_float2(sza0, sza1));
+            const float2 gzB = fmul2(fmul2(two, frcp2(fadd2(RM, make_float2(RM.y, rm2)))), make_float2(szb0, szb1));
+            dz_half<NO>(gzA.x, gzA.y, z2a0, z2a1);
+            dz_half<NO>(gzB.x, gzB.y, z2b0, z2b1);
         }
-        float v10, v11, v40, v41;
+        float2 v1, v4;
         {
             float t0, t1, s0, s1;
             zc_coll<NO>(zz, t0, t1);
             zc_coll<NO>(zx, s0, s1);
-            v10 = ln0 * t0 * rdz * rdx; v11 = ln1 * t1 * rdz * rdx;
-            v40 = mn0 * s0 * rdz * rdx; v41 = mn1 * s1 * rdz * rdx;
+            v1 = fmul2(fmul2(fmul2(LNv, make_float2(t0, t1)), rdz), rdx);
+            v4 = fmul2(fmul2(fmul2(MNv, make_float2(s0, s1)), rdz), rdx);
         }
         float xzm0, xzm1, xzl0, xzl1;
-        dz_coll<NO>(mp0 * d20 * rdx, mp1 * d21 * rdx, xzm0, xzm1);
-        dz_coll<NO>(lp0 * d30 * rdx, lp1 * d31 * rdx, xzl0, xzl1);
+        const float2 am = fmul2(fmul2(MP, d2), rdx), al = fmul2(fmul2(LP, d3), rdx);
+        dz_coll<NO>(am.x, am.y, xzm0, xzm1);
+        dz_coll<NO>(al.x, al.y, xzl0, xzl1);
+        const float2 z2a = make_float2(z2a0, z2a1), z2b = make_float2(z2b0, z2b1);
+        const float2 xzm = make_float2(xzm0, xzm1), xzl = make_float2(xzl0, xzl1);
 
         // --- force chain
-        float ex0 = 0.f, ex1 = 0.f, ez0 = 0.f, ez1 = 0.f;
+        float2 ex = zero2, ez = zero2;
 #pragma unroll
         for (int i = 0; i < NF; ++i) {
-            float fx0 = FX[i][0], fx1 = FX[i][1], fz0 = FZ[i][0], fz1 = FZ[i][1];
+            float2 fx = FX[i], fz = FZ[i];
 #pragma unroll
             for (int k = 1; k <= NO; ++k) {
                 if (i == NO - k) {
-                    fx0 = fmaf(c_stag[NO][k], ga0, fx0); fx1 = fmaf(c_stag[NO][k], ga1, fx1);
-                    fz0 = fmaf(c_stag[NO][k], gb0, fz0); fz1 = fmaf(c_stag[NO][k], gb1, fz1);
+                    fx = ffma2(c_stag[NO][k], ga, fx);
+                    fz = ffma2(c_stag[NO][k], gb, fz);
                 }
                 if (i == NO - 1 + k) {
-                    fx0 = fmaf(-c_stag[NO][k], ga0, fx0); fx1 = fmaf(-c_stag[NO][k], ga1, fx1);
-                    fz0 = fmaf(-c_stag[NO][k], gb0, fz0); fz1 = fmaf(-c_stag[NO][k], gb1, fz1);
+                    fx = ffma2(-c_stag[NO][k], ga, fx);
+                    fz = ffma2(-c_stag[NO][k], gb, fz);
                 }
                 if (i == LAG - k) {
-                    fx0 = fmaf(c_coll[NO][k], v10, fx0); fx1 = fmaf(c_coll[NO][k], v11, fx1);
-                    fz0 = fmaf(c_coll[NO][k], v40, fz0); fz1 = fmaf(c_coll[NO][k], v41, fz1);
+                    fx = ffma2(c_coll[NO][k], v1, fx);
+                    fz = ffma2(c_coll[NO][k], v4, fz);
                 }
                 if (i == LAG + k) {
-                    fx0 = fmaf(-c_coll[NO][k], v10, fx0); fx1 = fmaf(-c_coll[NO][k], v11, fx1);
-                    fz0 = fmaf(-c_coll[NO][k], v40, fz0); fz1 = fmaf(-c_coll[NO][k], v41, fz1);
+                    fx = ffma2(-c_coll[NO][k], v1, fx);
+                    fz = ffma2(-c_coll[NO][k], v4, fz);
                 }
             }
             if (i == LAG) {
-                fx0 = fmaf(z2b0, dz2, fx0); fx1 = fmaf(z2b1, dz2, fx1);
-                fz0 = fmaf(z2a0, dz2, fz0); fz1 = fmaf(z2a1, dz2, fz1);
+                fx = ffma2(z2b, make_float2(dz2, dz2), fx);
+                fz = ffma2(z2a, make_float2(dz2, dz2), fz);
             }
             if (i == NO - 1) {
-                fx0 = fmaf(xzm0, rdz, fx0); fx1 = fmaf(xzm1, rdz, fx1);
-                fz0 = fmaf(xzl0, rdz, fz0); fz1 = fmaf(xzl1, rdz, fz1);
+                fx = ffma2(xzm, make_float2(rdz, rdz), fx);
+                fz = ffma2(xzl, make_float2(rdz, rdz), fz);
             }
             if (i == 0) {
-                ex0 = fx0; ex1 = fx1; ez0 = fz0; ez1 = fz1;
+                ex = fx; ez = fz;
             } else {
-                FX[i - 1][0] = fx0; FX[i - 1][1] = fx1; FZ[i - 1][0] = fz0; FZ[i - 1][1] = fz1;
+                FX[i - 1] = fx; FZ[i - 1] = fz;
             }
         }
-        FX[NF - 1][0] = FX[NF - 1][1] = FZ[NF - 1][0] = FZ[NF - 1][1] = 0.f;
+        FX[NF - 1] = FZ[NF - 1] = zero2;
 
         // cell xc is complete
         if (emit && store) {
             const float2 k2 = rdB(mc, 0), xp = rdB(mc, 1), zp = rdB(mc, 2);
             const float2 xo = rdA(xc, 0), zo = rdA(xc, 1);
-            float2 nxv, nzv;
-            nxv.x = fmaf(k2.x, ex0, 2.0f * xo.x - xp.x);
-            nxv.y = fmaf(k2.y, ex1, 2.0f * xo.y - xp.y);
-            nzv.x = fmaf(k2.x, ez0, 2.0f * zo.x - zp.x);
-            nzv.y = fmaf(k2.y, ez1, 2.0f * zo.y - zp.y);
+            // 2 u^n - u^{n-1} is exact before its rounding, so one FMA gives it
+            const float2 nxv = ffma2(k2, ex, ffma2(two, xo, make_float2(-xp.x, -xp.y)));
+            const float2 nzv = ffma2(k2, ez, ffma2(two, zo, make_float2(-zp.x, -zp.y)));
             const int oc = gofs(xc);
             if (store1) {
                 *reinterpret_cast<float2*>(uxn + oc) = nxv;
@@ -304,8 +289,8 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
             }
         }
 
-        rlp0 = rlq0; rlp1 = rlq1; rmp0 = rmq0; rmp1 = rmq1;
-        lp0 = lq0; lp1 = lq1; mp0 = mq0; mp1 = mq1;
+        RLP = RLQ; RMP = RMQ;
+        LP = LQv; MP = MQv;
     }
     cp_wait<0>();
 }
