@@ -163,6 +163,8 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
     float2 LP = rdA(c0, 2), MP = rdA(c0, 3);
     float2 RLP = frcp2(ffma2(two, MP, LP)), RMP = frcp2(MP);
 
+    // two columns per trip: the values carried to the next column alternate registers instead of moving
+#pragma unroll 2
     for (int mc = m0; mc <= m1; ++mc) {
         issue(mc + RG::kAhead);
         cp_wait<RG::kAhead>();                  // column mc has landed
