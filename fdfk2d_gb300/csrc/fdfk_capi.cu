@@ -8,6 +8,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -705,9 +706,9 @@ int fdfk_session_get_tuning(const fdfk_session* s, int* seg_len, int* pml_run)
 int fdfk_autotune(const fdfk_params* p, const float* c, int steps, int* seg_len, int* pml_run, float* ms_per_step)
 {
     if (!p || !c || !seg_len || !pml_run || steps < 1) return fail(FDFK_EINVAL, "bad argument");
-    const int segs[] = {16, 24, 32, 48, 64, 96};
     const int runs[] = {16, 24, 32, 48};
-    const int trials = 6 + 4;
+    std::vector<int> segs = {16, 24, 32, 48, 64, 96};
+    const int trials = (int)segs.size() + 2 + 4;
     fdfk_params q = *p;
     q.nt = trials * (steps + 2) + 1;
     fdfk_session* s = nullptr;
@@ -741,6 +742,16 @@ int fdfk_autotune(const fdfk_params* p, const float* c, int steps, int* seg_len,
         ms /= steps;
         return FDFK_OK;
     };
+    // plus the shortest segments that fill exactly one and two waves of resident fast-path warps
+    // (a partly filled last wave leaves SMs idle at the end of the step)
+    if (s->march.n_bands > 0) {
+        const int slots = march_warp_slots(q.norder);
+        for (int waves = 1; waves <= 2 && slots > 0; ++waves) {
+            int len = 16;
+            while (len < 1024 && (long long)((q.nx + len - 1) / len) * s->march.n_bands > (long long)waves * slots) ++len;
+            if (std::find(segs.begin(), segs.end(), len) == segs.end()) segs.push_back(len);
+        }
+    }
     int best_seg = s->march.n_bands > 0 ? s->march.seg_len : 0, best_run = s->pml_run;
     float best = 1e30f, ms = 0.f;
     if (s->march.n_bands > 0)
