@@ -706,9 +706,9 @@ int fdfk_session_get_tuning(const fdfk_session* s, int* seg_len, int* pml_run)
 int fdfk_autotune(const fdfk_params* p, const float* c, int steps, int* seg_len, int* pml_run, float* ms_per_step)
 {
     if (!p || !c || !seg_len || !pml_run || steps < 1) return fail(FDFK_EINVAL, "bad argument");
-    const int runs[] = {16, 24, 32, 48};
+    const int runs[] = {12, 16, 24, 32, 48};
     std::vector<int> segs = {16, 24, 32, 48, 64, 96};
-    const int trials = (int)segs.size() + 2 + 4;
+    const int trials = (int)segs.size() + 2 + 5;
     fdfk_params q = *p;
     q.nt = trials * (steps + 2) + 1;
     fdfk_session* s = nullptr;

@@ -137,8 +137,10 @@ int fdfk_session_set_tuning(fdfk_session* s, int seg_len, int pml_run);
 int fdfk_session_get_tuning(const fdfk_session* s, int* seg_len, int* pml_run);
 
 /*
- * Autotuner: times candidate launch shapes (segment lengths 16..96, tile
- * lengths 16..48) for sessions of parameters p and material c on a scratch
+ * Autotuner: times candidate launch shapes (segment lengths 16..96 and the
+ * shortest ones that fill one and two whole waves of fast-path warps;
+ * absorbing-layer tile lengths 12..48) for sessions of parameters p and
+ * material c on a scratch
  * session (zero state and background, `steps` timed steps per candidate,
  * CUDA events) and returns the fastest, for fdfk_session_set_tuning.
  */

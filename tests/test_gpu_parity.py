@@ -206,9 +206,9 @@ def test_tuning_changes_no_result(F):
     p = dict(d["p"])
     strips = {k: d[k] for k in F.STRIPS}
     seg, run, ms = F.autotune(p, d["c"], steps=5)
-    assert seg >= 16 and 16 <= run <= 48 and ms > 0
+    assert seg >= 16 and 12 <= run <= 48 and ms > 0
     out = []
-    for tune in ((0, 0), (16, 16), (96, 48), (seg, run)):
+    for tune in ((0, 0), (16, 12), (96, 48), (seg, run)):
         with F.Session(p, d["c"]) as s:
             s.set_tuning(*tune)
             s.upload_background(strips)
