@@ -334,30 +334,43 @@ __device__ __forceinline__ cd series_bin(const FkGeom& g, const SeriesTab& tab, 
 //   Z_k = E_k + i O_k,  E_k = X_k + conj(X_{M-k}),  O_k = (X_k - conj(X_{M-k})) exp(+2 pi i k / N),
 // sum_k Z_k exp(+2 pi i k m / M) = x[2m] + i x[2m+1], x the length-N real inverse transform of X.
 // The complex output read as doubles is therefore x itself.
+__device__ __forceinline__ cd fold_bin(cd xk, cd xm, cd t)   // t = exp(-2 pi i k / N)
+{
+    const cd e = mk(xk.x + xm.x, xk.y - xm.y);
+    const cd d = mk(xk.x - xm.x, xk.y + xm.y);
+    const cd o = mk(d.x * t.x + d.y * t.y, d.y * t.x - d.x * t.y);   // d * conj(t)
+    return mk(e.x - o.y, e.y + o.x);
+}
+
+// One block row per series, one thread per bin pair (k, M - k), k = 0..M/2: each spectral bin is
+// formed once and feeds both Z_k and Z_{M-k}.
 __global__ void fk_assemble(FkGeom g, SeriesTab tab, long long g0, int nb, const cd* __restrict__ U,
                             const cd* __restrict__ Ph, const double* __restrict__ cosphi, const cd* __restrict__ tw,
                             cd* __restrict__ spec)
 {
+    __shared__ SeriesPos sp;
     const int b = blockIdx.y;
+    if (b >= nb) return;
+    if (threadIdx.x == 0) sp = decode(tab, g0 + b);
+    __syncthreads();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int M = g.nh;
-    if (b >= nb || k >= M) return;
-    cd z = mk(0.0, 0.0);
+    if (k > M / 2) return;
+    cd* const row = spec + (size_t)b * M;
     if (k < g.K || M - k < g.K) {
-        const SeriesPos p = decode(tab, g0 + b);
+        const SeriesPos p = sp;
         cd xk = series_bin(g, tab, p, k, U, Ph, cosphi);
         cd xm = series_bin(g, tab, p, M - k, U, Ph, cosphi);
         if (k == 0) {
             xk.y = 0.0;
             xm.y = 0.0;
         }
-        const cd e = mk(xk.x + xm.x, xk.y - xm.y);
-        const cd d = mk(xk.x - xm.x, xk.y + xm.y);
-        const cd t = tw[k];                                 // exp(-2 pi i k / N)
-        const cd o = mk(d.x * t.x + d.y * t.y, d.y * t.x - d.x * t.y);   // d * conj(t)
-        z = mk(e.x - o.y, e.y + o.x);
+        row[k] = fold_bin(xk, xm, tw[k]);
+        if (k > 0 && 2 * k < M) row[M - k] = fold_bin(xm, xk, tw[M - k]);
+    } else {
+        row[k] = mk(0.0, 0.0);
+        if (2 * k < M) row[M - k] = mk(0.0, 0.0);
     }
-    spec[(size_t)b * M + k] = z;
 }
 
 // strips[s][q + per_s * n] = float(y[b][n] * escale[n]), n = 0..nt; 32 x 32 tiles through shared memory.
@@ -729,7 +742,7 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
     FK_CK(B.alloc(reinterpret_cast<char**>(&work), std::max(plan_full.work, plan_tail.work)));
     for (long long g0 = 0; g0 < nseries; g0 += nb_full) {
         const int nb = (int)std::min<long long>(nb_full, nseries - g0);
-        const dim3 ga((g.nh + 255) / 256, nb);
+        const dim3 ga((g.nh / 2 + 1 + 255) / 256, nb);
         fk_assemble<<<ga, 256, 0, stream>>>(g, tab, g0, nb, d_U, d_Ph, d_cos, d_tw, d_spec);
         const Z2ZPlan& pl = nb == nb_full ? plan_full : plan_tail;
         FFT_CK(cufftSetWorkArea(pl.h, work));
