@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -146,25 +147,60 @@ void free_session(fdfk_session* s)
     delete s;
 }
 
+// The FD coefficient tables in constant memory, uploaded once per device (they depend on nothing
+// but the order): a later session neither repeats the copy nor waits for the device.
+cudaError_t ensure_coefficients()
+{
+    static std::mutex mu;
+    static std::vector<char> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+    if (done[dev]) return cudaSuccess;
+    float stag[kMaxOrder + 1][kMaxOrder + 1], coll[kMaxOrder + 1][kMaxOrder + 1];
+    fd_tables(stag, coll);
+    e = set_coefficients(&stag[0][0], &coll[0][0]);
+    if (e == cudaSuccess) done[dev] = 1;
+    return e;
+}
+
 // Material planes from c(3, NZ, NX): the raw array is copied to the device (stream-ordered
-// scratch) and converted there (launch_material), then the validity flags are read back.
-int upload_material(fdfk_session* s, const float* c)
+// scratch) and converted there (launch_material), then the validity flags are read back.  This
+// runs on a stream of the highest priority, so that the wait for the flags does not queue behind
+// long kernels of other sessions (an FK background, a batch) already on the device; the session's
+// stream is ordered after it by an event.  `fresh`: the planes are new and nothing on the session's
+// stream uses them yet; otherwise the upload first waits for the session's stream.
+int upload_material(fdfk_session* s, const float* c, bool fresh)
 {
     const size_t nc = 3 * (size_t)s->NZ * s->NX;
+    int lo = 0, hi = 0;
+    cudaStream_t up = nullptr;
+    cudaEvent_t done = nullptr;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&up, cudaStreamNonBlocking, hi);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+    if (!fresh && e == cudaSuccess) e = cudaEventRecord(done, s->stream);
+    if (!fresh && e == cudaSuccess) e = cudaStreamWaitEvent(up, done, 0);
     float* d_c = nullptr;
     int* d_flag = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&d_c, nc * sizeof(float), s->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_flag, sizeof(int), s->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_flag, 0, sizeof(int), s->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_c, c, nc * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_c, nc * sizeof(float), up);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&d_flag, sizeof(int), up);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_flag, 0, sizeof(int), up);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_c, c, nc * sizeof(float), cudaMemcpyHostToDevice, up);
     if (e == cudaSuccess)
-        e = launch_material(d_c, s->NZ, s->NX, s->ldz, s->p.dt * s->p.dt, s->kdt2, s->lam, s->mu, d_flag, s->stream);
+        e = launch_material(d_c, s->NZ, s->NX, s->ldz, s->p.dt * s->p.dt, s->kdt2, s->lam, s->mu, d_flag, up);
     int flag = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream);
-    if (d_c) cudaFreeAsync(d_c, s->stream);
-    if (d_flag) cudaFreeAsync(d_flag, s->stream);
-    const cudaError_t e2 = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, up);
+    if (d_c) cudaFreeAsync(d_c, up);
+    if (d_flag) cudaFreeAsync(d_flag, up);
+    if (e == cudaSuccess) e = cudaEventRecord(done, up);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, done, 0);
+    const cudaError_t e2 = up ? cudaStreamSynchronize(up) : cudaSuccess;
     if (e == cudaSuccess) e = e2;
+    if (done) cudaEventDestroy(done);
+    if (up) cudaStreamDestroy(up);
     if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("material upload: ") + cudaGetErrorString(e));
     g_launches += 1;
     if (flag & 1) return fail(FDFK_EINVAL, "density must be positive everywhere");
@@ -283,16 +319,16 @@ int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out
 #undef AL
     s->have_bg.assign(p->nt + 1, 0);
 
-    float stag[kMaxOrder + 1][kMaxOrder + 1], coll[kMaxOrder + 1][kMaxOrder + 1];
-    fd_tables(stag, coll);
-    cudaError_t e = set_coefficients(&stag[0][0], &coll[0][0]);
+    cudaError_t e = ensure_coefficients();
     if (e != cudaSuccess) { free_session(s); return fail(FDFK_ECUDA, std::string("coefficients: ") + cudaGetErrorString(e)); }
 
+    // Nothing below waits for other work on the device: the copies from pageable host memory are
+    // staged before each call returns, and the material conversion runs on its own stream.
     std::vector<DampCol> dx, dz;
     damping(*p, dx, dz);
-    if ((rc = upload_material(s, c)) != FDFK_OK) { free_session(s); return rc; }
-    if (cudaMemcpy(s->dampx, dx.data(), dx.size() * sizeof(DampCol), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(s->dampz, dz.data(), dz.size() * sizeof(DampCol), cudaMemcpyHostToDevice) != cudaSuccess) {
+    if ((rc = upload_material(s, c, true)) != FDFK_OK) { free_session(s); return rc; }
+    if (cudaMemcpyAsync(s->dampx, dx.data(), dx.size() * sizeof(DampCol), cudaMemcpyHostToDevice, s->stream) != cudaSuccess ||
+        cudaMemcpyAsync(s->dampz, dz.data(), dz.size() * sizeof(DampCol), cudaMemcpyHostToDevice, s->stream) != cudaSuccess) {
         free_session(s);
         return fail(FDFK_ECUDA, "damping upload failed");
     }
@@ -400,7 +436,9 @@ int fdfk_session_set_receivers(fdfk_session* s, int nrcv, const float* rx, const
         CK(cudaMemcpyAsync(s->rz, rz, nrcv * sizeof(float), cudaMemcpyHostToDevice, s->stream));
         CK(cudaMemsetAsync(s->seisx, 0, ns * sizeof(float), s->stream));
         CK(cudaMemsetAsync(s->seisz, 0, ns * sizeof(float), s->stream));
-        CK(cudaStreamSynchronize(s->stream));
+        // no wait: copies from pageable memory are staged before the call returns, and everything
+        // that reads these arrays is ordered after them on the session's stream (a batch waits for
+        // the stream when the session joins), so an FK background still running is not waited for
     }
     // the sampling clock restarts with the loop (src/FDFK2D.f90:315-316)
     s->isis = s->istp * nstp;
@@ -982,7 +1020,7 @@ void updatedispl_(const int* norder, const int* nx, const int* nz, const int* np
         fdfk_session_destroy(g_legacy);
         g_legacy = nullptr;
         if (fdfk_session_create(&p, c, &g_legacy)) die("session create failed");
-    } else if (upload_material(g_legacy, c)) {
+    } else if (upload_material(g_legacy, c, false)) {
         die("material upload failed");
     }
     // the strips of this call, time index *it, uploaded as time 0 of a one-sample session
