@@ -394,7 +394,17 @@ int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out
 int fdfk_session_set_stream(fdfk_session* s, void* stream)
 {
     if (!s) return fail(FDFK_EINVAL, "session is NULL");
-    s->stream = (cudaStream_t)stream;
+    const cudaStream_t ns = (cudaStream_t)stream;
+    if (ns != s->stream) {
+        // work already queued on the old stream (the state cleared at creation, uploads) comes first
+        cudaEvent_t ev = nullptr;
+        CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        cudaError_t e = cudaEventRecord(ev, s->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ns, ev, 0);
+        cudaEventDestroy(ev);
+        if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("set_stream: ") + cudaGetErrorString(e));
+    }
+    s->stream = ns;
     return FDFK_OK;
 }
 

@@ -67,7 +67,8 @@ long long fdfk_kernel_launches(void);
  */
 int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out);
 
-/* Bind the session to a CUDA stream (cudaStream_t passed as void*; NULL = default). */
+/* Bind the session to a CUDA stream (cudaStream_t passed as void*; NULL = default).
+ * Work already queued on the previous stream is ordered before the new one's. */
 int fdfk_session_set_stream(fdfk_session* s, void* stream);
 
 /*
