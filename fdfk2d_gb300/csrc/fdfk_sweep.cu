@@ -26,6 +26,11 @@ namespace fdfk {
 __constant__ float c_stag[kMaxOrder + 1][kMaxOrder + 1];  // [n][j]: fd_coef0(j, n), zero for j > n
 __constant__ float c_coll[kMaxOrder + 1][kMaxOrder + 1];  // [n][j]: fd_coef1(j, n)
 
+// Free-surface forcing terms of a row-1 cell, formed once per column of a tile that holds row 1:
+// the interior update's (Dx[lam dz uz] and the half-row stress term of each component, added in
+// that order), and the split-field update's F2 and F3 of each component.
+enum { kFsA, kFsQx, kFsB, kFsQz, kFsF2x, kFsF3x, kFsF2z, kFsF3z, kFsTerms };
+
 // Shared-memory layout of a TZ x TX tile (z fastest) for stencil half-order NO.
 struct TileDims {
     int TZ, TX;
@@ -34,6 +39,7 @@ struct TileDims {
     int MZ, MX;     // material tile
     int XW, ZW;     // extents of the x- / z-consumed arrays
     int U, M, AX, AZ;
+    int FS;         // free-surface terms of row 1 (kFsTerms per column)
     int total;      // floats
 };
 
@@ -47,7 +53,8 @@ __host__ __device__ __forceinline__ TileDims tile_dims(int NO, int TZ, int TX)
     t.XW = TX + 2 * NO; t.ZW = TZ + 2 * NO;
     t.U = t.UZ * t.UX; t.M = t.MZ * t.MX;
     t.AX = TZ * t.XW; t.AZ = t.ZW * TX;
-    t.total = 2 * t.U + 4 * t.M + 4 * t.AX + 4 * t.AZ;
+    t.FS = kFsTerms * TX;
+    t.total = 2 * t.U + 4 * t.M + 4 * t.AX + 4 * t.AZ + t.FS;
     return t;
 }
 
@@ -263,6 +270,7 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
     float* gzB = gzA + T.AZ;   // H(mu)  * Dstag_z(ux)
     float* v2 = gzB + T.AZ;    // mu  * Dx(uz)/dx        [x][z]  (dxz(mu uz))
     float* v3 = v2 + T.AZ;     // lam * Dx(ux)/dx                 (dxz(lam ux))
+    float* sFS = v3 + T.AZ;    // free-surface terms of row 1       [term][x]
 
     const float rdx = 1.0f / a.dx, rdz = 1.0f / a.dz;
     const float* uxc = a.ux[a.cur];
@@ -335,6 +343,53 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
 
 #define SU(arr, z, x) arr[((x) + H) * T.UZ + ((z) + H)]
 #define SM(arr, z, x) arr[((x) + NO) * T.MZ + ((z) + NO)]
+
+    // ---- free surface (row 1, stress image about row 1.5): its terms per column, once -------
+    // Formed here by one thread per column rather than inside the output loop, where the row-1
+    // cells of a warp would hold every other lane idle through the divisions.
+    if (R.z0 == 1) {
+        const float dx = a.dx, dz = a.dz;
+        for (int x = tid; x < TX; x += kThreads) {
+            const int nxo = ordx(a, R.x0 + x, NO);
+            float dA = 0.f, dB = 0.f, dz1 = 0.f, dz2v = 0.f, dx1 = 0.f, dx2v = 0.f;
+#pragma unroll
+            for (int k = 1; k <= NO; ++k) {
+                float c = c_coll[nxo][k];
+                float Ap = SM(sLam, 0, x + k) * (SU(suz, 1, x + k) - SU(suz, 0, x + k)) / dz;
+                float Am = SM(sLam, 0, x - k) * (SU(suz, 1, x - k) - SU(suz, 0, x - k)) / dz;
+                float Bp = SM(sMu, 0, x + k) * (SU(sux, 1, x + k) - SU(sux, 0, x + k)) / dz;
+                float Bm = SM(sMu, 0, x - k) * (SU(sux, 1, x - k) - SU(sux, 0, x - k)) / dz;
+                dA = fmaf(c, Ap - Am, dA);
+                dB = fmaf(c, Bp - Bm, dB);
+                dz1 = fmaf(c, SU(suz, 0, x + k) - SU(suz, 0, x - k), dz1);
+                dz2v = fmaf(c, SU(suz, 1, x + k) - SU(suz, 1, x - k), dz2v);
+                dx1 = fmaf(c, SU(sux, 0, x + k) - SU(sux, 0, x - k), dx1);
+                dx2v = fmaf(c, SU(sux, 1, x + k) - SU(sux, 1, x - k), dx2v);
+            }
+            dA /= dx; dB /= dx; dz1 /= dx; dz2v /= dx; dx1 /= dx; dx2v /= dx;
+            const float mu1 = SM(sMu, 0, x), mu2 = SM(sMu, 1, x);
+            const float la1 = SM(sLam, 0, x), la2 = SM(sLam, 1, x);
+            const float hmu = 2.0f / (SM(sRMu, 0, x) + SM(sRMu, 1, x));
+            const float hl2m = 2.0f / (SM(sRL2m, 0, x) + SM(sRL2m, 1, x));
+            const float dux = SU(sux, 1, x) - SU(sux, 0, x);
+            const float duz = SU(suz, 1, x) - SU(suz, 0, x);
+            const float fsA = dA;                                   // Dx[lam(1) dz uz]
+            const float fsB = dB;                                   // Dx[mu(1)  dz ux]
+            const float fsx = hmu * dux / dz;                       // z part of sxz(1.5)
+            const float fsz = hl2m * duz / dz;                      // z part of szz(1.5)
+            // x parts of the half-row stresses
+            const float dux1 = 0.5f * (mu1 * dz1 + mu2 * dz2v);     // (mu1 Dx uz1 + mu2 Dx uz2)/2
+            const float duz1 = 0.5f * (la1 * dx1 + la2 * dx2v);     // (lam1 Dx ux1 + lam2 Dx ux2)/2
+            sFS[kFsA * TX + x] = fsA;
+            sFS[kFsQx * TX + x] = 2.0f * (fsx + dux1) / dz;
+            sFS[kFsB * TX + x] = fsB;
+            sFS[kFsQz * TX + x] = 2.0f * (fsz + duz1) / dz;
+            sFS[kFsF2x * TX + x] = fsA + 2.0f * dux1 / dz;
+            sFS[kFsF3x * TX + x] = 2.0f * fsx / dz;
+            sFS[kFsF2z * TX + x] = fsB + 2.0f * duz1 / dz;
+            sFS[kFsF3z * TX + x] = 2.0f * fsz / dz;
+        }
+    }
 
     // ---- phase 1a: x-direction staggered products and dzx operands -----------
     Walk w1(tid, TZ, kThreads);
@@ -422,7 +477,6 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
 #define VZI(arr, z, x) arr[(x) * T.ZW + ((z) + NO)]
 
     // ---- phase 2: output cells ----------------------------------------------
-    const float dx = a.dx, dz = a.dz;
     const float dx2 = pml ? a.dx2p : a.dx2r;
     Walk wc(tid, TZ, kThreads);
     for (int cell = tid; cell < TZ * TX; cell += kThreads, wc.next()) {
@@ -513,40 +567,6 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         const float Fzx_lam_uz = zxl * rdx, Fzx_mu_ux = zxm * rdx;
         const float Fxz_mu_uz = xzm * rdz, Fxz_lam_ux = xzl * rdz;
 
-        // free-surface terms on row 1 (stress image about row 1.5)
-        float fsA = 0.f, fsB = 0.f, fsx = 0.f, fsz = 0.f, dux1 = 0.f, duz1 = 0.f;
-        if (iz == 1) {
-            float dA = 0.f, dB = 0.f, dz1 = 0.f, dz2v = 0.f, dx1 = 0.f, dx2v = 0.f;
-#pragma unroll
-            for (int k = 1; k <= NO; ++k) {
-                float c = c_coll[nxo][k];
-                float Ap = SM(sLam, 0, x + k) * (SU(suz, 1, x + k) - SU(suz, 0, x + k)) / dz;
-                float Am = SM(sLam, 0, x - k) * (SU(suz, 1, x - k) - SU(suz, 0, x - k)) / dz;
-                float Bp = SM(sMu, 0, x + k) * (SU(sux, 1, x + k) - SU(sux, 0, x + k)) / dz;
-                float Bm = SM(sMu, 0, x - k) * (SU(sux, 1, x - k) - SU(sux, 0, x - k)) / dz;
-                dA = fmaf(c, Ap - Am, dA);
-                dB = fmaf(c, Bp - Bm, dB);
-                dz1 = fmaf(c, SU(suz, 0, x + k) - SU(suz, 0, x - k), dz1);
-                dz2v = fmaf(c, SU(suz, 1, x + k) - SU(suz, 1, x - k), dz2v);
-                dx1 = fmaf(c, SU(sux, 0, x + k) - SU(sux, 0, x - k), dx1);
-                dx2v = fmaf(c, SU(sux, 1, x + k) - SU(sux, 1, x - k), dx2v);
-            }
-            dA /= dx; dB /= dx; dz1 /= dx; dz2v /= dx; dx1 /= dx; dx2v /= dx;
-            const float mu1 = SM(sMu, 0, x), mu2 = SM(sMu, 1, x);
-            const float la1 = SM(sLam, 0, x), la2 = SM(sLam, 1, x);
-            const float hmu = 2.0f / (SM(sRMu, 0, x) + SM(sRMu, 1, x));
-            const float hl2m = 2.0f / (SM(sRL2m, 0, x) + SM(sRL2m, 1, x));
-            const float dux = SU(sux, 1, x) - SU(sux, 0, x);
-            const float duz = SU(suz, 1, x) - SU(suz, 0, x);
-            fsA = dA;                                   // Dx[lam(1) dz uz]
-            fsB = dB;                                   // Dx[mu(1)  dz ux]
-            fsx = hmu * dux / dz;                       // z part of sxz(1.5)
-            fsz = hl2m * duz / dz;                      // z part of szz(1.5)
-            // x parts of the half-row stresses
-            dux1 = 0.5f * (mu1 * dz1 + mu2 * dz2v);     // (mu1 Dx uz1 + mu2 Dx uz2)/2
-            duz1 = 0.5f * (la1 * dx1 + la2 * dx2v);     // (lam1 Dx ux1 + lam2 Dx ux2)/2
-        }
-
         float* uxn = a.ux[a.cur ^ 1];
         float* uzn = a.uz[a.cur ^ 1];
         const float ux0 = uxc[g], uz0 = uzc[g];
@@ -554,8 +574,8 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         if (!pml) {
             float Fx, Fz;
             if (iz == 1) {
-                Fx = Fx2_l2m_ux + fsA + 2.0f * (fsx + dux1) / dz;
-                Fz = Fx2_mu_uz + fsB + 2.0f * (fsz + duz1) / dz;
+                Fx = Fx2_l2m_ux + sFS[kFsA * TX + x] + sFS[kFsQx * TX + x];
+                Fz = Fx2_mu_uz + sFS[kFsB * TX + x] + sFS[kFsQz * TX + x];
             } else {
                 Fx = Fx2_l2m_ux + Fzx_lam_uz + Fz2_mu_ux + Fxz_mu_uz;
                 Fz = Fz2_l2m_uz + Fxz_lam_ux + Fx2_mu_uz + Fzx_mu_ux;
@@ -617,13 +637,13 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             if (iz == 1) {
                 if (comp == 0) {
                     F1 = Fx2_l2m_ux;
-                    F2 = fsA + 2.0f * dux1 / dz;
-                    F3 = 2.0f * fsx / dz;
+                    F2 = sFS[kFsF2x * TX + x];
+                    F3 = sFS[kFsF3x * TX + x];
                     S1 = l2m0 * dxux;
                 } else {
                     F1 = Fx2_mu_uz;
-                    F2 = fsB + 2.0f * duz1 / dz;
-                    F3 = 2.0f * fsz / dz;
+                    F2 = sFS[kFsF2z * TX + x];
+                    F3 = sFS[kFsF3z * TX + x];
                     S1 = mu0 * dxuz;
                 }
             } else if (comp == 0) {
