@@ -280,14 +280,16 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
     // kFill items per thread per round: every load of a round is issued before the first
     // shared-memory store, so a round costs one memory latency.
     constexpr int kFill = 4;
+    Walk wu(tid, T.UZ, kThreads);     // (i % UZ, i / UZ) of this thread's items, in order
     for (int i0 = tid; i0 < T.U; i0 += kFill * kThreads) {
         float vx[kFill], vz[kFill], bx[kFill], bz[kFill];
 #pragma unroll
         for (int q = 0; q < kFill; ++q) {
             const int i = i0 + q * kThreads;
+            const int sz = wu.r, sx = wu.q;
+            wu.next();
             vx[q] = 0.f; vz[q] = 0.f; bx[q] = 0.f; bz[q] = 0.f;
             if (i < T.U) {
-                const int sz = i % T.UZ, sx = i / T.UZ;
                 const int iz = R.z0 - H + sz, ix = R.x0 - H + sx;
                 if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
                     const size_t g = gidx(a, iz, ix);
@@ -311,14 +313,16 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             }
         }
     }
+    Walk wm(tid, T.MZ, kThreads);
     for (int i0 = tid; i0 < T.M; i0 += kFill * kThreads) {
         float l[kFill], m[kFill];
 #pragma unroll
         for (int q = 0; q < kFill; ++q) {
             const int i = i0 + q * kThreads;
+            const int mz = wm.r, mx = wm.q;
+            wm.next();
             l[q] = 0.f; m[q] = 1.f;
             if (i < T.M) {
-                const int mz = i % T.MZ, mx = i / T.MZ;
                 const int iz = R.z0 - NO + mz, ix = R.x0 - NO + mx;
                 if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
                     const size_t g = gidx(a, iz, ix);
