@@ -732,13 +732,21 @@ int fdfk_session_set_tuning(fdfk_session* s, int seg_len, int pml_run)
     if (s->batch) return fail(FDFK_ESTATE, "the session is a member of a batch");
     if ((seg_len != 0 && (seg_len < 8 || seg_len > 1024)) || (pml_run != 0 && (pml_run < 8 || pml_run > 64)))
         return fail(FDFK_EINVAL, "segment length must be 8..1024 and tile length 8..64 (0 keeps the current)");
+    if (pml_run) {
+        // the tiles of that length must fit one block's shared memory (high orders, long runs)
+        StepArgs trial = s->base;
+        plan_tiles(trial, s->march.n_bands > 0, pml_run);
+        int dev = 0, optin = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        if (step_smem_for(trial) > (size_t)optin)
+            return fail(FDFK_EINVAL, "tile length " + std::to_string(pml_run) + " needs more shared memory than a block has");
+        s->pml_run = pml_run;
+        s->base = trial;
+    }
     if (seg_len && s->march.n_bands > 0) {
         s->march.seg_len = seg_len;
         s->march.n_segs = (s->p.nx + seg_len - 1) / seg_len;
-    }
-    if (pml_run) {
-        s->pml_run = pml_run;
-        plan_tiles(s->base, s->march.n_bands > 0, pml_run);
     }
     return FDFK_OK;
 }
@@ -808,7 +816,10 @@ int fdfk_autotune(const fdfk_params* p, const float* c, int steps, int* seg_len,
             if (ms < best) { best = ms; best_seg = seg; }
         }
     for (int run : runs) {
-        if ((rc = time_it(best_seg, run, ms))) return rc;
+        if ((rc = time_it(best_seg, run, ms))) {
+            if (rc == FDFK_EINVAL) continue;          // tiles too large for this order: not a candidate
+            return rc;
+        }
         if (ms < best) { best = ms; best_run = run; }
     }
     *seg_len = best_seg;

@@ -217,3 +217,21 @@ def test_tuning_changes_no_result(F):
             out.append(s.seismograms())
     for sx, sz in out[1:]:
         assert np.array_equal(sx, out[0][0]) and np.array_equal(sz, out[0][1])
+
+
+def test_tuning_rejects_tiles_beyond_shared_memory(F):
+    """At the highest order, 64-cell runs across a 40-cell layer need more shared memory than a
+    block has: set_tuning refuses them (and keeps the current shapes), and the autotuner skips
+    such candidates."""
+    from test_gpu_batch import _layered
+    nx, nz, npml, h = 40, 30, 40, 250.0
+    c, fk, vmax = _layered(nx, nz, npml, h, 3000.0)
+    p = dict(norder=8, nx=nx, nz=nz, npml=npml, nbd=15, nt=10, dx=h, dz=h, dt=0.004, vpml=vmax, npower=2, R0=1e-3)
+    with F.Session(p, c) as s:
+        before = s.tuning()
+        with pytest.raises(F.FDFKError):
+            s.set_tuning(0, 64)
+        assert s.tuning() == before
+        s.set_tuning(0, 16)
+    seg, run, ms = F.autotune(p, c, steps=2)
+    assert 12 <= run <= 48 and ms > 0
