@@ -159,7 +159,7 @@ def _random_state(seed, p):
     return ux, uz, bp, bu, strips
 
 
-def _gpu_step(F, p, c, state, tiled_only):
+def _gpu_step(F, p, c, state, tiled_only, seg=0):
     import os
     ux, uz, bp, bu, strips = [x.copy() if isinstance(x, np.ndarray) else {k: v.copy(order="F") for k, v in x.items()}
                               for x in state]
@@ -168,6 +168,8 @@ def _gpu_step(F, p, c, state, tiled_only):
     os.environ["FDFK_TILED_ONLY"] = "1" if tiled_only else "0"
     try:
         with F.Session(p, c) as s:
+            if seg:
+                s.set_tuning(seg, 0)
             s.upload_background(strips)
             s.upload_state(ux, uz, bp, bu, 0)
             s.advance(1)
@@ -235,3 +237,26 @@ def test_tuning_rejects_tiles_beyond_shared_memory(F):
         s.set_tuning(0, 16)
     seg, run, ms = F.autotune(p, c, steps=2)
     assert 12 <= run <= 48 and ms > 0
+
+
+@pytest.mark.parametrize("nx,nz,npml,seg", [(10, 8, 5, 0),      # two fast-path rows, one short segment
+                                            (97, 53, 5, 16),    # one partial band, ragged last segment, minimum layer
+                                            (131, 59, 9, 24),   # a second band holding one row
+                                            (64, 121, 7, 64)])  # segment length equal to nx
+def test_ragged_shapes_fast_path_matches_tiled_path_and_oracle(F, oracle_lib, nx, nz, npml, seg):
+    """Order 6 on grids whose rows and columns do not divide into the fast path's bands and
+    segments, including the thinnest absorbing layer (material columns left of the grid)."""
+    norder = 3
+    p, c, _, _, _ = _random_case(nx + nz, nx, nz, npml, norder, 0)
+    state = _random_state(nx * nz, p)
+    mx, mz = _gpu_step(F, p, c, state, tiled_only=False, seg=seg)
+    tx, tz = _gpu_step(F, p, c, state, tiled_only=True)
+    assert max_rel(mx, tx) < STEP_TOL
+    assert max_rel(mz, tz) < STEP_TOL
+    ux, uz, bp, bu, strips = state
+    ox, oz = ux.copy(order="F"), uz.copy(order="F")
+    oracle_lib.updatedispl(dict(p, izt=1, nbd=2 * norder - 1), strips, c, oracle_lib.fd_coef0(norder),
+                           oracle_lib.fd_coef1(norder), ox, oz, {k: v.copy(order="F") for k, v in bp.items()},
+                           {k: v.copy(order="F") for k, v in bu.items()}, 0)
+    assert max_rel(mx, ox) < STEP_TOL
+    assert max_rel(mz, oz) < STEP_TOL
