@@ -8,7 +8,9 @@
 // (fdfk_march_ring.cuh).  The x-direction stencils are evaluated in
 // transposed (accumulator) form: every incoming column is folded with one FMA
 // per stencil tap into a short chain of partial sums that advances with the
-// march, so no operand windows are kept or shifted.  z-direction stencils
+// march, so no operand windows are kept or shifted.  The two rows of a lane go
+// through the same operations, so each such FMA (and each per-row product) is
+// one packed FP32x2 instruction for both rows, rounded per row as fmaf.  z-direction stencils
 // read neighbouring rows with warp shuffles, one shuffle per distinct
 // neighbour row.  There is no block-level synchronisation.  The 2*norder halo
 // rows on each side of a band are computed but not stored; bands overlap
