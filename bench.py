@@ -250,7 +250,9 @@ def batched_and_served(F, WL, args, torch, dev):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    # default: the workload's whole record (nt = 12000 -> 12001 steps), so that e2e is one full solve
+    # and the clock sampler sees more than a second of load
+    ap.add_argument("--steps", type=int, default=12001)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="config2", choices=["config2", "config1"])
