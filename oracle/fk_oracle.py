@@ -233,3 +233,75 @@ def background(p, bazs, fk_left, fk_right, x0=0.0, z0=0.0, dtype=np.float32):
             arr[:, jj, :] = (xt[:nt + 1].T * np.exp(alpha * tn) / N).astype(dtype)
         out[name] = arr
     return out
+
+
+def background_device(p, bazs, fk_left, fk_right, x0=0.0, z0=0.0, device="cuda", chunk_bytes=1 << 30):
+    """:func:`background` in FP64 with the per-column inverse transforms batched on a torch device.
+
+    Same mathematics as :func:`background` (same spectrum, response, phase, fold and scaling): the
+    layered response is evaluated only at the kept frequencies (k <= 10 f0 N dt; the others are
+    zero in both), and the inverse transform of the Hermitian spectrum is a real inverse FFT.
+    Returns dict name -> float64 tensor of shape (nt+1, n2, n1), C-contiguous: the bytes of the
+    reference's Fortran strip (n1, n2, nt+1).  Used for the FP64 oracle at full workload sizes.
+    """
+    import torch
+    nx, nz, npml, nbd, nt, dt = p["nx"], p["nz"], p["npml"], p["nbd"], p["nt"], p["dt"]
+    dx, dz = p["dx"], p["dz"]
+    W, N, alpha = source_spectrum(nt, dt, p["f0"], p["ds"])
+    nh = N // 2
+    kmax = min(nh - 1, int(np.floor(10.0 * float(np.float32(p["f0"])) * N * dt)))
+    w = 2.0 * np.pi * np.arange(nh + 1) / (N * dt)
+    wc = (w - 1j * alpha)[:kmax + 1]
+    inc = "P" if p["src_type"] else "S"
+    ray = float(p["rayp"])
+    x_c = x0 + 0.5 * (nx - 1) * dx
+    half = 0.5 * (nx - 1) * dx
+    cbar = np.cos(np.sum(np.asarray(bazs, np.float64)) / (nx + 2 * npml + 1))
+    r_ref = half * abs(cbar)
+    z_ref = z0 + (nz - 1) * dz
+    tn = torch.arange(nt + 1, dtype=torch.float64, device=device) * dt
+    damp = torch.exp(alpha * tn)
+    Wt = torch.as_tensor(W[:kmax + 1], device=device)
+    wct = torch.as_tensor(wc, device=device)
+    out = {}
+    cache = {}
+    for name in STRIPS:
+        iz, ix = strip_coords(nx, nz, nbd, name)
+        side = name[2]
+        res = torch.empty((nt + 1, len(ix), len(iz)), dtype=torch.float64, device=device)
+        groups = {}
+        for jj, cx in enumerate(ix):
+            if side == "b":
+                left = cx <= nbd if cbar >= 0.0 else cx <= nx - nbd
+            else:
+                left = side == "l"
+            groups.setdefault(bool(left), []).append(jj)
+        for left, cols in groups.items():
+            model = fk_left if left else fk_right
+            key = (id(model), tuple(iz))
+            if key not in cache:
+                UR, UZ = layered_response(model, ray, wc, z0 + (iz - 1) * dz, inc, z_ref)
+                cache[key] = (torch.as_tensor(UR, device=device), torch.as_tensor(UZ, device=device))
+            UR, UZ = cache[key]
+            per_col = (nh + 1) * len(iz) * 16 + N * len(iz) * 8
+            step = max(1, int(chunk_bytes // per_col))
+            for a in range(0, len(cols), step):
+                cj = cols[a:a + step]
+                cxs = np.asarray([ix[j] for j in cj])
+                phi = np.asarray(bazs, np.float64)[cxs - 1 + npml]
+                xs = x0 + (cxs - 1) * dx
+                arg = torch.as_tensor(ray * (np.cos(phi) * (xs - x_c) - r_ref), device=device)
+                ph = torch.exp(1j * wct[:, None] * arg[None, :])                       # (K, C)
+                if name[1] == "x":
+                    U = UR[:, :, None] * torch.as_tensor(np.cos(phi), device=device)[None, None, :]
+                else:
+                    U = UZ[:, :, None].expand(-1, -1, len(cj))
+                X = torch.zeros((nh + 1, len(iz), len(cj)), dtype=torch.complex128, device=device)
+                X[:kmax + 1] = Wt[:, None, None] * U * ph[:, None, :]
+                xt = torch.fft.irfft(X, n=N, dim=0) * N                                  # (N, R, C)
+                del X
+                v = xt[:nt + 1] * damp[:, None, None] / N
+                res[:, cj[0]:cj[-1] + 1, :] = v.permute(0, 2, 1)
+                del xt, v
+        out[name] = res
+    return out

@@ -11,6 +11,8 @@ use this module.  It loads ``oracle/_build/libfdfk_oracle.so`` (built by
 * :func:`simulate64` - the same time loop with every field in FP64
   (``oracle/_build/libfdfk_oracle64.so``): the FP64 oracle the FP32 traces are
   stated against;
+* :func:`simulate64_gpu` - the same FP64 time loop on the GPU
+  (``oracle/_build/libfdfk_oracle_gpu.so``), for the full-size workloads;
 * :func:`fd_coef0` / :func:`fd_coef1` / :func:`fd_coef2` (src/Submain.f90:1111-1245).
 
 Array conventions match ``oracle/refharness.py``.
@@ -168,3 +170,77 @@ def simulate(p, strips, c, rx, rz, x0, z0, nstp, nsis, steps_limit=-1):
     if rc != 0:
         raise RuntimeError(f"oracle simulate failed: {rc}")
     return seisx, seisz
+
+
+LIBGPU = os.path.join(HERE, "_build", "libfdfk_oracle_gpu.so")
+
+
+class ParamsGpu(C.Structure):
+    _fields_ = [("norder", C.c_int), ("nx", C.c_int), ("nz", C.c_int), ("npml", C.c_int), ("izt", C.c_int),
+                ("npower", C.c_int), ("nbd", C.c_int), ("nt", C.c_int), ("dx", C.c_double), ("dz", C.c_double),
+                ("dt", C.c_double), ("vpml", C.c_double), ("R0", C.c_double)]
+
+
+_libgpu = None
+
+
+def libgpu():
+    """oracle/_build/libfdfk_oracle_gpu.so: the FP64 GPU oracle (oracle/fdfk_oracle_gpu.cu)."""
+    global _libgpu
+    if _libgpu is None:
+        if not os.path.exists(LIBGPU):
+            build()
+        _libgpu = C.CDLL(LIBGPU)
+        _libgpu.fdfk_oracle_gpu_simulate.restype = C.c_int
+    return _libgpu
+
+
+def strips_to_device(strips, device="cuda"):
+    """Twelve background strips as float64 tensors on the GPU in the reference's memory layout.
+
+    A strip of Fortran shape (n1, n2, nt+1) becomes a C-contiguous tensor of shape (nt+1, n2, n1),
+    the same bytes.  Tensors already on the device pass through (they must have that form)."""
+    import torch
+    out = {}
+    for k in STRIPS:
+        a = strips[k]
+        if isinstance(a, torch.Tensor):
+            t = a.to(device=device, dtype=torch.float64)
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.float64).transpose(2, 1, 0))).to(device)
+        out[k] = t.contiguous()
+    return out
+
+
+def simulate64_gpu(p, strips, c, rx, rz, x0, z0, nstp, nsis, steps_limit=-1, fields=False):
+    """The restated time loop in FP64 on the GPU (oracle/fdfk_oracle_gpu.cu).
+
+    strips: numpy arrays in the reference layout, or float64 CUDA tensors of shape (nt+1, n2, n1)
+    (see :func:`strips_to_device`).  Returns float64 (seisx, seisz) of shape (nsis+1, nrcv), and
+    with fields=True also level 1 of ux, uz after the last step, shape (nz+npml, nx+2npml)."""
+    import torch
+    L = libgpu()
+    dev = strips_to_device(strips)
+    sp = (C.c_void_p * 12)(*[C.c_void_p(dev[k].data_ptr()) for k in STRIPS])
+    nrcv = len(rx)
+    seisx = np.zeros((nsis + 1, nrcv), np.float64, order="F")
+    seisz = np.zeros((nsis + 1, nrcv), np.float64, order="F")
+    cf = np.asfortranarray(c, np.float32)
+    rxa = np.ascontiguousarray(rx, np.float64)
+    rza = np.ascontiguousarray(rz, np.float64)
+    NZ, NX = int(p["nz"]) + int(p["npml"]), int(p["nx"]) + 2 * int(p["npml"])
+    ux = np.zeros((NZ, NX), np.float64, order="F") if fields else None
+    uz = np.zeros((NZ, NX), np.float64, order="F") if fields else None
+    prm = ParamsGpu(int(p["norder"]), int(p["nx"]), int(p["nz"]), int(p["npml"]), int(p.get("izt", 1)),
+                    int(p.get("npower", 2)), int(p["nbd"]), int(p["nt"]), float(p["dx"]), float(p["dz"]),
+                    float(p["dt"]), float(p["vpml"]), float(p.get("R0", 1e-3)))
+    torch.cuda.synchronize()
+    rc = L.fdfk_oracle_gpu_simulate(C.byref(prm), sp, cf.ctypes.data_as(C.c_void_p), C.c_int(nrcv),
+                                    rxa.ctypes.data_as(C.c_void_p), rza.ctypes.data_as(C.c_void_p), C.c_double(x0),
+                                    C.c_double(z0), C.c_int(nstp), C.c_int(nsis), seisx.ctypes.data_as(C.c_void_p),
+                                    seisz.ctypes.data_as(C.c_void_p), C.c_int(steps_limit),
+                                    ux.ctypes.data_as(C.c_void_p) if fields else None,
+                                    uz.ctypes.data_as(C.c_void_p) if fields else None)
+    if rc != 0:
+        raise RuntimeError(f"FP64 GPU oracle simulate failed: {rc}")
+    return (seisx, seisz, ux, uz) if fields else (seisx, seisz)

@@ -66,3 +66,18 @@ def test_bottom_strip_model_switch():
         for j in range(a.shape[1]):
             ref = al if j < left_cols else ar
             assert np.array_equal(a[:, j], ref[:, j]), (baz, j)
+
+
+@pytest.mark.parametrize("name", ("fk_p_ramp", "fk_s_left"))
+def test_batched_restatement_matches_per_column(name):
+    """background_device (the batched form used for the full-size FP64 oracle, here on the CPU with
+    small chunks) gives the per-column restatement's FP64 values to rounding."""
+    d = load_npz(name)
+    p = d["p"]
+    a = FO.background(p, d["bazs"], d["fk_left"], d["fk_right"], x0=p["x0"], z0=p["z0"], dtype=np.float64)
+    b = FO.background_device(p, d["bazs"], d["fk_left"], d["fk_right"], x0=p["x0"], z0=p["z0"], device="cpu",
+                             chunk_bytes=1 << 16)
+    for k in FO.STRIPS:
+        got = b[k].numpy().transpose(2, 1, 0)
+        assert got.shape == a[k].shape, k
+        assert max_rel(got, a[k]) < 1e-12, k
