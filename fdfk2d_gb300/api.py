@@ -222,10 +222,11 @@ class Session:
         _check(lib().fdfk_session_advance(self._h, C.c_int(nsteps)))
 
     def advance_timed(self, nsteps: int):
-        """Advance with CUDA events around each kernel; returns (ms_interior, ms_edge) summed."""
-        ti, te = C.c_float(), C.c_float()
-        _check(lib().fdfk_session_advance_timed(self._h, C.c_int(nsteps), C.byref(ti), C.byref(te)))
-        return float(ti.value), float(te.value)
+        """Advance with CUDA events around each kernel; returns (ms_interior, ms_edge, ms_total): the
+        summed times of the fast-path and tiled kernels and the time of all the steps, from one loop."""
+        ti, te, tt = C.c_float(), C.c_float(), C.c_float()
+        _check(lib().fdfk_session_advance_timed(self._h, C.c_int(nsteps), C.byref(ti), C.byref(te), C.byref(tt)))
+        return float(ti.value), float(te.value), float(tt.value)
 
     def cell_split(self):
         """(cells on the interior fast path, cells on the tiled kernel) per step."""

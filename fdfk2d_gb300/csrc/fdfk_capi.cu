@@ -21,6 +21,7 @@
 namespace fdfk {
 cudaError_t launch_step(const StepArgs& a, cudaStream_t s);
 cudaError_t launch_march(const StepArgs& a, const MarchArgs& m, cudaStream_t s);
+cudaError_t launch_march_marked(const StepArgs& a, const MarchArgs& m, cudaStream_t s, cudaEvent_t after_frame);
 int march_warp_slots(int norder);
 cudaError_t set_coefficients(const float* stag, const float* coll);
 }  // namespace fdfk
@@ -505,18 +506,22 @@ int fdfk_session_advance(fdfk_session* s, int nsteps)
     return FDFK_OK;
 }
 
-int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, float* ms_edge)
+int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, float* ms_edge, float* ms_total)
 {
     if (!s || !ms_interior || !ms_edge) return fail(FDFK_EINVAL, "NULL argument");
     if (s->batch) return fail(FDFK_ESTATE, "the session is a member of a batch; advance the batch");
     *ms_interior = 0.f;
     *ms_edge = 0.f;
+    if (ms_total) *ms_total = 0.f;
     if (nsteps <= 0) return fdfk_session_advance(s, nsteps);
     const bool two = s->march.n_bands > 0;
-    std::vector<cudaEvent_t> ev((size_t)nsteps * 4, nullptr);
+    // all events exist before the first step is queued, so their creation is not timed
+    std::vector<cudaEvent_t> ev((size_t)nsteps * 4 + 2, nullptr);
     auto cleanup = [&]() { for (auto e : ev) if (e) cudaEventDestroy(e); };
     for (auto& e : ev)
         if (cudaEventCreate(&e) != cudaSuccess) { cleanup(); return fail(FDFK_ECUDA, "event creation failed"); }
+    cudaEvent_t t_begin = ev[(size_t)nsteps * 4], t_end = ev[(size_t)nsteps * 4 + 1];
+    cudaEventRecord(t_begin, s->stream);
     for (int k = 0; k < nsteps; ++k) {
         const int it = s->it;
         if (it > s->p.nt) { cleanup(); return fail(FDFK_EINVAL, "advance past the last time index nt"); }
@@ -545,8 +550,8 @@ int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, 
         cudaError_t r = launch_edge(s, a, edge, &nl);
         cudaEventRecord(e[3], edge);
         if (r == cudaSuccess && two) {
-            cudaEventRecord(e[0], s->stream);
-            r = launch_march(a, s->march, s->stream);
+            // e[0] .. e[1] brackets the fast-path kernel alone (the frame kernel runs before e[0])
+            r = launch_march_marked(a, s->march, s->stream, e[0]);
             cudaEventRecord(e[1], s->stream);
             cudaEventRecord(s->join, s->side);
             cudaStreamWaitEvent(s->stream, s->join, 0);
@@ -556,7 +561,12 @@ int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, 
         s->cur ^= 1;
         s->it += 1;
     }
+    cudaEventRecord(t_end, s->stream);
     if (cudaStreamSynchronize(s->stream) != cudaSuccess) { cleanup(); return fail(FDFK_ECUDA, "synchronize failed"); }
+    if (ms_total) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, t_begin, t_end) == cudaSuccess) *ms_total = t;
+    }
     double ti = 0.0, te = 0.0;
     for (int k = 0; k < nsteps; ++k) {
         float t = 0.f;
@@ -990,11 +1000,12 @@ int fdfk_step_noalloc(const fdfk_params* p, int it, const float* const strips[12
     for (int k = 0; k < 18; ++k)
         if (!bu[k]) return fail(FDFK_EINVAL, "bu array is NULL");
     if (it < 0 || it > p->nt) return fail(FDFK_EINVAL, "it outside 0..nt");
-    float stag[kMaxOrder + 1][kMaxOrder + 1], coll[kMaxOrder + 1][kMaxOrder + 1];
-    fd_tables(stag, coll);
+    // the coefficient tables, once per device (later calls neither copy nor wait)
+    const cudaError_t ce = ensure_coefficients();
+    if (ce != cudaSuccess) return fail(FDFK_ECUDA, std::string("coefficient tables: ") + cudaGetErrorString(ce));
     std::string err;
     long long nl = 0;
-    rc = step_noalloc(*p, it, strips, c, ux, uz, bp, bu, &stag[0][0], &coll[0][0], (cudaStream_t)stream, err, &nl);
+    rc = step_noalloc(*p, it, strips, c, ux, uz, bp, bu, (cudaStream_t)stream, err, &nl);
     g_launches += nl;
     if (rc) return fail(rc, err);
     return FDFK_OK;
@@ -1012,6 +1023,37 @@ long long fdfk_step_noalloc_need(const fdfk_params* p)
 // gfortran-ABI drop-in
 // ---------------------------------------------------------------------------
 static fdfk_session* g_legacy = nullptr;
+static std::mutex g_legacy_mu;
+
+// True when the caller's coef0/coef1 (real(8) coef(norder, norder), src/Submain.f90:1111-1200:
+// fd_coef0 staggered, fd_coef1 collocated, every reduced order) are the tables this library
+// computes itself; the step uses its own tables, so different ones must not pass silently.
+static bool caller_coefficients_match(int norder, const double* coef0, const double* coef1)
+{
+    for (int n = 1; n <= norder; ++n)
+        for (int j = 1; j <= norder; ++j) {
+            double st = 0.0, co = 0.0;
+            if (j <= n) {
+                double num = 1.0, den = 1.0, numc = 1.0, denc = 1.0;
+                const double aj = (double)((2 * j - 1) * (2 * j - 1)), bj = (double)(j * j);
+                for (int k = 1; k <= n; ++k) {
+                    if (k == j) continue;
+                    const double ak = (double)((2 * k - 1) * (2 * k - 1)), bk = (double)(k * k);
+                    num *= ak;
+                    den *= (k < j) ? (aj - ak) : (ak - aj);
+                    numc *= bk;
+                    denc *= (k < j) ? (bj - bk) : (bk - bj);
+                }
+                const double sgn = (j % 2 == 1) ? 1.0 : -1.0;
+                st = sgn * num / (den * (double)(2 * j - 1));
+                co = sgn * numc / (denc * 2.0 * (double)j);
+            }
+            const size_t i = (size_t)(j - 1) + (size_t)(n - 1) * (size_t)norder;
+            if (std::fabs(coef0[i] - st) > 1e-12 * std::fabs(st) + 1e-300) return false;
+            if (std::fabs(coef1[i] - co) > 1e-12 * std::fabs(co) + 1e-300) return false;
+        }
+    return true;
+}
 
 void updatedispl_(const int* norder, const int* nx, const int* nz, const int* npml, const int* izt,
                   const int* is_PML_top, const int* npower, const int* nbd, const int* it, const int* nt,
@@ -1027,7 +1069,8 @@ void updatedispl_(const int* norder, const int* nx, const int* nz, const int* np
                   float* bux1b, float* bux2b, float* bux3b, float* buz1b, float* buz2b, float* buz3b,
                   float* bux1t, float* bux2t, float* bux3t, float* buz1t, float* buz2t, float* buz3t)
 {
-    (void)coef0; (void)coef1;  // the weights are regenerated from their closed form
+    // one legacy session per process: calls from several host threads take turns
+    std::lock_guard<std::mutex> lock(g_legacy_mu);
     fdfk_params p{};
     p.norder = *norder; p.nx = *nx; p.nz = *nz; p.npml = *npml; p.is_PML_top = *is_PML_top ? 1 : 0;
     p.npower = *npower; p.nbd = *nbd; p.nt = 0; p.dx = *dx; p.dz = *dz; p.dt = *dt; p.vpml = *vpml; p.R0 = *R0;
@@ -1036,6 +1079,11 @@ void updatedispl_(const int* norder, const int* nx, const int* nz, const int* np
         std::abort();
     };
     if (*izt != 1 || p.is_PML_top) { g_err = "is_PML_top"; die("only the free-surface top boundary is implemented"); }
+    if (p.norder < 1 || p.norder > kMaxOrder) { g_err = "norder"; die("stencil order outside 1..8"); }
+    if (!caller_coefficients_match(p.norder, coef0, coef1)) {
+        g_err = "coef0/coef1";
+        die("coef0/coef1 are not the fd_coef0/fd_coef1 tables of this order");
+    }
     const bool same = g_legacy && std::memcmp(&g_legacy->p, &p, sizeof(p)) == 0;
     if (!same) {
         fdfk_session_destroy(g_legacy);

@@ -307,13 +307,15 @@ cudaError_t launch_march_batch_fast(const BatchTab& t, int norder, int blocks, c
     }
 }
 
-// The frame of the step, then the fast path (two launches).
-cudaError_t launch_march(const StepArgs& a, const MarchArgs& m, cudaStream_t s)
+// The frame of the step, then the fast path (two launches); `after_frame` (if not null) is
+// recorded on the stream between them.
+cudaError_t launch_march_marked(const StepArgs& a, const MarchArgs& m, cudaStream_t s, cudaEvent_t after_frame)
 {
     if (m.n_bands <= 0 || m.n_segs <= 0) return cudaSuccess;
     fdfk_frame_kernel<<<frame_blocks(a), kFrameThreads, 0, s>>>(a);
-    const cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (after_frame && (e = cudaEventRecord(after_frame, s)) != cudaSuccess) return e;
     switch (a.norder) {
     case 1: return launch_march_no<1>(a, m, s);
     case 2: return launch_march_no<2>(a, m, s);
@@ -321,6 +323,12 @@ cudaError_t launch_march(const StepArgs& a, const MarchArgs& m, cudaStream_t s)
     case 4: return launch_march_no<4>(a, m, s);
     default: return cudaErrorInvalidValue;
     }
+}
+
+// The frame of the step, then the fast path (two launches).
+cudaError_t launch_march(const StepArgs& a, const MarchArgs& m, cudaStream_t s)
+{
+    return launch_march_marked(a, m, s, nullptr);
 }
 
 }  // namespace fdfk

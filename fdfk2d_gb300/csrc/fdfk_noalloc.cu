@@ -15,8 +15,15 @@
 // drained, so consecutive calls from one thread are safe on any streams.
 //
 // First-call setup: the first call on a device resolves the scratch address
-// with cudaGetSymbolAddress (which also loads this module); make one call on
-// each device before any stream capture begins on it.
+// with cudaGetSymbolAddress (which also loads this module) and caches it for
+// that device; any failed CUDA call in this path drops the cached address, so
+// the next call resolves it again (after a device reset the first call may
+// fail once with FDFK_ECUDA).  No call may be made on a stream that is being
+// captured, nor while any global-mode capture is in progress: every call does
+// pageable copies and waits for its stream.
+//
+// The FD coefficient tables go to constant memory once per device, before
+// this path runs (the caller, fdfk_step_noalloc, sees to it).
 #include "fdfk_gb300.h"
 #include "fdfk_noalloc.cuh"
 #include "fdfk_sweep.cuh"
@@ -30,7 +37,6 @@
 namespace fdfk {
 
 cudaError_t launch_step(const StepArgs& a, cudaStream_t s);
-cudaError_t set_coefficients(const float* stag, const float* coll);
 
 namespace {
 
@@ -38,6 +44,13 @@ __device__ __align__(256) float g_na_scratch[kNoAllocFloats];
 
 constexpr int kMaxDevices = 64;
 float* g_na_base[kMaxDevices] = {};
+
+// Drops the cached scratch address of the current device (after a failed CUDA call).
+void na_forget()
+{
+    int d = -1;
+    if (cudaGetDevice(&d) == cudaSuccess && d >= 0 && d < kMaxDevices) g_na_base[d] = nullptr;
+}
 DampCol g_na_dampx[kNoAllocMaxDim];
 DampCol g_na_dampz[kNoAllocMaxDim];
 
@@ -142,6 +155,7 @@ __global__ void na_pack_bu(DeintTab t, int npml, int NX)
         cudaError_t e_ = (call);                                                                 \
         if (e_ != cudaSuccess) {                                                                 \
             err = std::string(#call) + ": " + cudaGetErrorString(e_);                            \
+            na_forget();                                                                         \
             return FDFK_ECUDA;                                                                   \
         }                                                                                        \
     } while (0)
@@ -171,8 +185,7 @@ size_t noalloc_floats_needed(const fdfk_params& p)
 }
 
 int step_noalloc(const fdfk_params& p, int it, const float* const strips[12], const float* c, float* ux, float* uz,
-                 float* const bp[12], float* const bu[24], const float* stag, const float* coll, cudaStream_t st,
-                 std::string& err, long long* launches)
+                 float* const bp[12], float* const bu[24], cudaStream_t st, std::string& err, long long* launches)
 {
     const int NZ = p.nz + p.npml, NX = p.nx + 2 * p.npml, ldz = (NZ + 31) / 32 * 32;
     const size_t n = (size_t)ldz * NX;
@@ -232,8 +245,7 @@ int step_noalloc(const fdfk_params& p, int it, const float* const strips[12], co
     for (int k = 0; k < 18; ++k) rbu[k] = take(2 * (k < 12 ? side : tb));
     int* flag = reinterpret_cast<int*>(take(64));
 
-    // coefficients and damping profile (the closed forms of the session path)
-    NA_CK(set_coefficients(stag, coll));
+    // damping profile (the closed form of the session path)
     {
         const double lg = std::log(1.0 / p.R0);
         const double Lx = (double)p.npml * p.dx, Lz = (double)p.npml * p.dz;

@@ -18,10 +18,10 @@ constexpr int kNoAllocMaxDim = 1 << 16;
 // Scratch floats one step of this geometry needs (every region rounded up to 256 bytes).
 size_t noalloc_floats_needed(const fdfk_params& p);
 
-// One step of updatedispl_ semantics on the static scratch; `p` already validated.
+// One step of updatedispl_ semantics on the static scratch; `p` already validated and the FD
+// coefficient tables already in constant memory on the current device.
 int step_noalloc(const fdfk_params& p, int it, const float* const strips[12], const float* c, float* ux, float* uz,
-                 float* const bp[12], float* const bu[24], const float* stag, const float* coll, cudaStream_t st,
-                 std::string& err, long long* launches);
+                 float* const bp[12], float* const bu[24], cudaStream_t st, std::string& err, long long* launches);
 
 // Material planes from the reference's material array c(3, NZ, NX) (rho, lambda, mu) on the
 // device: dt^2/rho, lambda, mu with leading dimension ldz (rows NZ..ldz-1 padding: 0, 0, 1).  Sets

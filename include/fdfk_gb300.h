@@ -97,9 +97,11 @@ int fdfk_session_advance(fdfk_session* s, int nsteps);
  * fdfk_session_advance with a CUDA-event pair around every kernel launch (on
  * the stream that launches it), then a synchronize: *ms_interior is the summed
  * time of the interior fast-path kernel, *ms_edge that of the tiled kernel
- * (top rows, absorbing layers, receivers).  Measurement only.
+ * (top rows, absorbing layers, receivers), and *ms_total (if not NULL) the
+ * time of all nsteps steps between two events on the session's stream, so the
+ * kernels' times and the steps' time come from the same loop.  Measurement only.
  */
-int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, float* ms_edge);
+int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, float* ms_edge, float* ms_total);
 
 /* Cells per step handled by the interior fast path and by the tiled kernel. */
 int fdfk_session_interior_cells(const fdfk_session* s, long long* interior, long long* edge);
@@ -384,7 +386,12 @@ void comput_background_wavefield_(const int* nx, const int* nz, const int* npml,
  * Races: the scratch is shared by every caller in the process on a device;
  * calls that overlap in time (two host threads, or two streams) corrupt each
  * other - serialise them.  The first call on a device resolves the scratch
- * address (cudaGetSymbolAddress); make it before any stream capture begins.
+ * address (cudaGetSymbolAddress) and the FD coefficient tables go to constant
+ * memory once per device; a failed CUDA call drops the cached address, so after
+ * a device reset the first call may fail once and the next resolves it again.
+ * No call may be made on a stream that is being captured, nor while any
+ * global-mode stream capture is in progress: each call does pageable copies
+ * and waits for its stream.
  */
 int fdfk_step_noalloc(const fdfk_params* p, int it, const float* const strips[12], const float* c, float* ux,
                       float* uz, float* const bp[12], float* const bu[24], void* stream);

@@ -82,3 +82,33 @@ def test_fk_entry_points_validate_without_gpu(built):
         F.fk_background(p, np.zeros(5), m, m)
     with pytest.raises(ValueError):
         F.fk_background(p, baz, m[:3], m)
+
+
+def test_noalloc_source_names_no_allocating_call():
+    """The allocation-free step's source file, and the bodies of the helpers it launches through,
+    name no device allocation or release and no library call that allocates."""
+    import re
+    csrc = os.path.join(ROOT, "fdfk2d_gb300", "csrc")
+    forbidden = re.compile(r"\b(cudaMalloc\w*|cudaFree\w*|cuMemAlloc\w*|cuMemFree\w*|cufft\w*|cublas\w*|"
+                           r"cudaMemPool\w*|cudaHostAlloc|cudaHostRegister|malloc|calloc|realloc|new\b)")
+    src = open(os.path.join(csrc, "fdfk_noalloc.cu")).read()
+    code = re.sub(r"//[^\n]*|/\*.*?\*/", "", src, flags=re.S)
+    assert not forbidden.findall(code), forbidden.findall(code)
+
+    def body(fname, sig):
+        text = re.sub(r"//[^\n]*|/\*.*?\*/", "", open(os.path.join(csrc, fname)).read(), flags=re.S)
+        i = text.index(sig)
+        j = text.index("{", i)
+        depth = 0
+        for k in range(j, len(text)):
+            depth += {"{": 1, "}": -1}.get(text[k], 0)
+            if depth == 0:
+                return text[j:k + 1]
+        raise AssertionError(sig)
+
+    for fname, sig in (("fdfk_sweep.cu", "cudaError_t launch_step(const StepArgs& a, cudaStream_t s)"),
+                       ("fdfk_sweep.cu", "cudaError_t set_coefficients(const float* stag, const float* coll)"),
+                       ("fdfk_capi.cu", "cudaError_t ensure_coefficients()"),
+                       ("fdfk_capi.cu", "int fdfk_step_noalloc(")):
+        b = body(fname, sig)
+        assert not forbidden.findall(b), (sig, forbidden.findall(b))

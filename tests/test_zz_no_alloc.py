@@ -1,5 +1,12 @@
 """GPU: the allocation-free single-step entry point fdfk_step_noalloc, called through the C ABI,
-against the existing drop-in updatedispl_ on two calls in a row."""
+against the existing drop-in updatedispl_ on two calls in a row, and its first call against one
+step of the reference's shipped libraries.
+
+The entry point serves callers that cannot allocate device memory themselves: a host program that
+owns a fixed device budget, or code that runs where cudaMalloc is not allowed.  It carves every
+buffer from one static device array, so these tests also check that a call leaves the device's
+free memory unchanged.  This file is collected last, so a run that stops at the first failure has
+already run every other test; it passes alone in a fresh process as well."""
 import ctypes as C
 
 import numpy as np
@@ -39,23 +46,36 @@ def _noalloc(F, p, it, strips, c, ux, uz, bp, bu):
                                      None)
 
 
+# One FP32 GPU step vs one step of the reference's shipped library (the fixture's out_* arrays).
+SHIPPED_TOL = 2e-5
+
+
+def _compare(ux, uz, bp, bu, rux, ruz, rbp, rbu, tol):
+    assert max_rel(ux, rux) < tol
+    assert max_rel(uz, ruz) < tol
+    for k in bp:
+        if rbp[k].any():
+            assert max_rel(bp[k], rbp[k]) < tol, k
+    for k in bu:
+        if rbu[k].any():
+            assert max_rel(bu[k], rbu[k]) < tol, k
+
+
 @pytest.mark.parametrize("name", ("n3", "n1", "n2_odd", "n8", "n3_minpml_aniso"))
 def test_noalloc_step_matches_dropin_on_two_calls(F, name):
     d = load_npz("step_" + name)
     p, strips, c, c0, c1, ux, uz, bp, bu = step_inputs(d)
     ref = step_inputs(d)
     it = int(d["it"])
-    for _ in range(2):
+    for call in range(2):
         F.updatedispl(*ref[:9], it)
         assert _noalloc(F, p, it, strips, c, ux, uz, bp, bu) == 0, F.lib().fdfk_last_error()
-    assert max_rel(ux, ref[5]) < TOL
-    assert max_rel(uz, ref[6]) < TOL
-    for k in bp:
-        if ref[7][k].any():
-            assert max_rel(bp[k], ref[7][k]) < TOL, k
-    for k in bu:
-        if ref[8][k].any():
-            assert max_rel(bu[k], ref[8][k]) < TOL, k
+        if call == 0:
+            # the first call is one step of the shipped libHybrid/libPML from the same state
+            shipped_bp = {k: d["out_" + k] for k in bp}
+            shipped_bu = {k: d["out_" + k] for k in bu}
+            _compare(ux, uz, bp, bu, d["out_ux"], d["out_uz"], shipped_bp, shipped_bu, SHIPPED_TOL)
+        _compare(ux, uz, bp, bu, ref[5], ref[6], ref[7], ref[8], TOL)
 
 
 def test_noalloc_step_allocates_nothing(F):
