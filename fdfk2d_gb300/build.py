@@ -58,7 +58,7 @@ def build(verbose: bool = False, extra=()) -> str:
         for msg in ex.map(compile_one, zip(srcs, objs)):
             if verbose and msg:
                 print(msg, file=sys.stderr)
-    cmd = [cc, "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart", "-lcufft"]
+    cmd = [cc, "-shared", "-o", LIB + ".tmp"] + objs + ARCH + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

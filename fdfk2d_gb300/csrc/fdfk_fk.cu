@@ -1,27 +1,34 @@
-// FK background wavefield on the GPU in FP64 (replaces libFK3D's
-// comput_background_wavefield_, call site src/FDFK2D.f90:429-431).
+// FK background wavefield on the GPU (replaces libFK3D's comput_background_wavefield_, call
+// site src/FDFK2D.f90:429-431).  Spectra and responses in FP64; the frequency-to-time transform
+// in double-float (df64, about 48 bits) on the FP32 pipes.
 //
 // Pipeline (one stream):
 //   1. host: per-layer vertical slownesses, wave-vector matrices E (ux, uz,
 //      sigma_xz, sigma_zz per unit amplitude of down P, down S, up P, up S) and
 //      interface matrices C_j = E_j^-1 E_{j+1}; the damped Ricker samples;
-//   2. fk_source_dft: W_k, k <= kmax, direct DFT against an exact twiddle table;
+//   2. fk_source_dft: W_k, k <= kmax, direct DFT against an exact twiddle table (FP64);
 //   3. fk_layer_amps: one thread per (model, frequency) propagates the 4x4
 //      layer matrices from the half-space to the surface, solves the 2x2
 //      free-surface system for the downgoing half-space amplitudes and writes
-//      every layer's amplitudes (phase referenced at the layer top);
-//   4. fk_depth_response: U_R, U_Z per (model, grid row, frequency);
-//   5. fk_column_phase: W_k times the horizontal phase per (column, frequency);
-//   6. per batch of strip series: fk_assemble folds each half spectrum into
-//      the input of a half-length complex inverse FFT (batched Z2Z, cuFFT,
-//      in place) whose output is the real series, and
-//      fk_epilogue scales by exp(alpha t)/N and transposes into the strips
-//      (time slowest), float32.
+//      every layer's amplitudes (phase referenced at the layer top) (FP64);
+//   4. fk_depth_response: U_R, U_Z per (model, grid row, frequency), FP64, stored as df64;
+//   5. fk_column_phase: W_k times the horizontal phase per (column, frequency), FP64, stored
+//      as df64; fk_df_twiddles: the df64 twiddle tables;
+//   6. per batch of strip series: fk_transform forms each series' half spectrum, folds it into
+//      the input of a half-length complex inverse transform whose output is the real series
+//      itself, runs that transform in shared memory (Stockham radix 4, df64), scales by
+//      exp(alpha t)/N and writes the series as float; fk_epilogue transposes the batch into the
+//      strips (time slowest).
+//
+// Why df64: GB300's FP64 rate is a small fraction of its FP32 rate, and the transform is the
+// bulk of the arithmetic.  Plain FP32 is not enough: the output is multiplied by exp(alpha t),
+// up to e^10, so the transform's rounding must stay below about 1e-12 of the series' maximum;
+// df64's ~2^-48 unit roundoff over log2(M) stages keeps the strips within FP32 rounding of the
+// FP64 restatement.
+#include "fdfk_df64.cuh"
 #include "fdfk_fk.cuh"
 #include "fdfk_gb300.h"
 #include "fdfk_sweep.cuh"
-
-#include <cufft.h>
 
 #include <algorithm>
 #include <array>
@@ -269,7 +276,7 @@ __global__ void fk_layer_amps(FkGeom g, const FkLayer* __restrict__ lay0, const 
 // U[(m * nrow + row) * K + k] = {U_R, U_Z} at z = z0 + row dz.
 __global__ void fk_depth_response(FkGeom g, const FkLayer* __restrict__ lay0, const FkLayer* __restrict__ lay1,
                                   int L0, int L1, const cd* __restrict__ amp0, const cd* __restrict__ amp1, int nrow,
-                                  double z0, double dz, cd* __restrict__ U)
+                                  double z0, double dz, float4* __restrict__ U)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long total = 2LL * nrow * g.K;
@@ -293,13 +300,13 @@ __global__ void fk_depth_response(FkGeom g, const FkLayer* __restrict__ lay0, co
         ur = cadd(ur, cmul(e, Ly[j].E[0][q]));
         uz = cadd(uz, cmul(e, Ly[j].E[1][q]));
     }
-    U[2 * t] = ur;
-    U[2 * t + 1] = uz;
+    U[2 * t] = df64::from_double(ur.x, ur.y);
+    U[2 * t + 1] = df64::from_double(uz.x, uz.y);
 }
 
 // Ph[c * K + k] = W_k exp(i wc_k D_c), D_c = p (cos(baz_c) (x_c' - x_centre) - r_ref).
 __global__ void fk_column_phase(FkGeom g, int ncol, const double* __restrict__ D, const cd* __restrict__ W,
-                                cd* __restrict__ Ph)
+                                float4* __restrict__ Ph)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)ncol * g.K) return;
@@ -307,83 +314,212 @@ __global__ void fk_column_phase(FkGeom g, int ncol, const double* __restrict__ D
     const int c = (int)(t / g.K);
     const double d = D[c];
     const cd e = cexp_(mk(g.alpha * d, g.dw * k * d));
-    Ph[t] = cmul(W[k], e);
+    const cd v = cmul(W[k], e);
+    Ph[t] = df64::from_double(v.x, v.y);
 }
 
-// Half spectra of series [g0, g0 + nb): spec[b * (nh + 1) + k].
-// Bin j (0..nh) of the half spectrum of series p: W_j * phase * U (times cos(baz) for the x
-// component), zero from j = K on.
-__device__ __forceinline__ cd series_bin(const FkGeom& g, const SeriesTab& tab, const SeriesPos& p, int j,
-                                         const cd* __restrict__ U, const cd* __restrict__ Ph,
-                                         const double* __restrict__ cosphi)
+// df64 twiddle tables: twM[t] = exp(+2 pi i t / M), t < M (M = N / 2, the transform length) and
+// twN[k] = exp(+2 pi i k / N), k < M (the fold's half-bin rotation).
+__global__ void fk_df_twiddles(int M, float4* __restrict__ twM, float4* __restrict__ twN)
 {
-    if (j >= g.K) return mk(0.0, 0.0);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= M) return;
+    double s, c;
+    sincospi(2.0 * (double)t / (double)M, &s, &c);
+    twM[t] = df64::from_double(c, s);
+    sincospi((double)t / (double)M, &s, &c);
+    twN[t] = df64::from_double(c, s);
+}
+
+// Bin j of the half spectrum of series p (df64): W_j * phase * U (times cos(baz) for the x
+// component); zero from j = K on.
+__device__ __forceinline__ df64::C series_bin(const FkGeom& g, const SeriesTab& tab, const SeriesPos& p, int j,
+                                              const float4* __restrict__ U, const float4* __restrict__ Ph,
+                                              const float2* __restrict__ cosd)
+{
+    if (j >= g.K) return df64::zero();
     const int c = p.ix - (1 - tab.nbd);
     const bool xcomp = (p.s & 1) == 0;
-    const cd u = U[(((size_t)p.model * tab.nrow + (p.iz - 1)) * g.K + j) * 2 + (xcomp ? 0 : 1)];
-    cd v = cmul(Ph[(size_t)c * g.K + j], u);
+    const df64::C u = df64::unpack(__ldg(&U[(((size_t)p.model * tab.nrow + (p.iz - 1)) * g.K + j) * 2 + (xcomp ? 0 : 1)]));
+    df64::C v = df64::cmul(df64::unpack(__ldg(&Ph[(size_t)c * g.K + j])), u);
     if (xcomp) {
-        const double cp = cosphi[c];
-        v = mk(v.x * cp, v.y * cp);
+        const float2 cp = __ldg(&cosd[c]);
+        v = df64::cscale(v, cp.x, cp.y);
     }
     return v;
 }
 
-// Input of the half-length complex inverse transform that yields a batch of real series: with
-// M = N/2 and X the half spectrum (X_0 and X_M enter with their real parts, as for a real series),
+// Input of the half-length complex inverse transform that yields a real series: with M = N/2 and
+// X the half spectrum (X_0 and X_M enter with their real parts, as for a real series),
 //   Z_k = E_k + i O_k,  E_k = X_k + conj(X_{M-k}),  O_k = (X_k - conj(X_{M-k})) exp(+2 pi i k / N),
 // sum_k Z_k exp(+2 pi i k m / M) = x[2m] + i x[2m+1], x the length-N real inverse transform of X.
-// The complex output read as doubles is therefore x itself.
-__device__ __forceinline__ cd fold_bin(cd xk, cd xm, cd t)   // t = exp(-2 pi i k / N)
+__device__ __forceinline__ df64::C fold_bin(const df64::C& xk, const df64::C& xm, const float4& wN)
 {
-    const cd e = mk(xk.x + xm.x, xk.y - xm.y);
-    const cd d = mk(xk.x - xm.x, xk.y + xm.y);
-    const cd o = mk(d.x * t.x + d.y * t.y, d.y * t.x - d.x * t.y);   // d * conj(t)
-    return mk(e.x - o.y, e.y + o.x);
+    const df64::C cm = df64::conj(xm);
+    const df64::C e = df64::cadd(xk, cm);
+    const df64::C o = df64::cmul(df64::csub(xk, cm), df64::unpack(wN));
+    return df64::cadd(e, df64::times_i(o));
 }
 
-// One block row per series, one thread per bin pair (k, M - k), k = 0..M/2: each spectral bin is
-// formed once and feeds both Z_k and Z_{M-k}.
-__global__ void fk_assemble(FkGeom g, SeriesTab tab, long long g0, int nb, const cd* __restrict__ U,
-                            const cd* __restrict__ Ph, const double* __restrict__ cosphi, const cd* __restrict__ tw,
-                            cd* __restrict__ spec)
+// Z_k of series p (k < M); zero unless k < K or M - k < K.
+__device__ __forceinline__ df64::C fold_at(const FkGeom& g, const SeriesTab& tab, const SeriesPos& p, int k,
+                                           const float4* __restrict__ U, const float4* __restrict__ Ph,
+                                           const float2* __restrict__ cosd, const float4* __restrict__ twN)
 {
+    const int M = g.nh;
+    df64::C xk = series_bin(g, tab, p, k, U, Ph, cosd);
+    df64::C xm = k == 0 ? df64::zero() : series_bin(g, tab, p, M - k, U, Ph, cosd);
+    if (k == 0) {
+        xk.hi.y = 0.f;
+        xk.lo.y = 0.f;
+    }
+    return fold_bin(xk, xm, __ldg(&twN[k]));
+}
+
+template <int Q>
+struct TransformShape {
+    static constexpr int kThreads = Q >= 512 ? Q / 16 : 32;
+    static constexpr int kLog = Q <= 1 ? 0 : 1 + TransformShape<Q / 2>::kLog;
+};
+template <>
+struct TransformShape<1> {
+    static constexpr int kThreads = 32;
+    static constexpr int kLog = 0;
+};
+
+// One Stockham stage of radix R (inverse sign) on the Q-point df64 sequence in shared memory, in
+// place through registers: every thread reads all its butterflies' inputs, the block synchronises,
+// then every thread writes its outputs.  Ns = product of the radices of the stages before.
+// Twiddle w_{Ns R}^{kr} = w_M^{kr (Q / (Ns R)) P}.
+template <int Q, int R>
+__device__ __forceinline__ void stockham_stage(float4* sm, int Ns, int P, const float4* __restrict__ twM)
+{
+    constexpr int T = TransformShape<Q>::kThreads;
+    constexpr int J = Q / R;                     // butterflies
+    constexpr int BPT = (J + T - 1) / T;         // butterflies per thread
+    df64::C v[BPT][R];
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int j = threadIdx.x + t * T;
+        if (j < J) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[t][r] = df64::unpack(sm[j + r * J]);
+        }
+    }
+    __syncthreads();
+    const int step = Q / (Ns * R);
+#pragma unroll
+    for (int t = 0; t < BPT; ++t) {
+        const int j = threadIdx.x + t * T;
+        if (j < J) {
+            const int k = j & (Ns - 1);
+            if (k != 0) {
+#pragma unroll
+                for (int r = 1; r < R; ++r)
+                    v[t][r] = df64::cmul(v[t][r], df64::unpack(__ldg(&twM[(size_t)k * r * step * P])));
+            }
+            if constexpr (R == 2) {
+                const df64::C a = v[t][0], b = v[t][1];
+                v[t][0] = df64::cadd(a, b);
+                v[t][1] = df64::csub(a, b);
+            } else {
+                // inverse 4-point DFT: X_q = sum_n v_n i^{nq}
+                const df64::C a0 = df64::cadd(v[t][0], v[t][2]), a1 = df64::csub(v[t][0], v[t][2]);
+                const df64::C a2 = df64::cadd(v[t][1], v[t][3]), a3 = df64::times_i(df64::csub(v[t][1], v[t][3]));
+                v[t][0] = df64::cadd(a0, a2);
+                v[t][2] = df64::csub(a0, a2);
+                v[t][1] = df64::cadd(a1, a3);
+                v[t][3] = df64::csub(a1, a3);
+            }
+            const int d = (j / Ns) * Ns * R + k;
+#pragma unroll
+            for (int r = 0; r < R; ++r) sm[d + r * Ns] = df64::pack(v[t][r]);
+        }
+    }
+    __syncthreads();
+}
+
+// Series g0 + blockIdx.x, branch r = blockIdx.y of the M = P Q point inverse transform: with
+// m = P m' + r (decimation in time of the output),
+//   z_{P m' + r} = sum_{k' < Q} w_Q^{k' m'} [ w_M^{k' r} sum_{j < P} Z_{k' + Q j} w_P^{j r} ],
+// a Q-point transform per branch.  Writes x[n] exp(alpha t_n) / N, n = 2m, 2m + 1 <= nt, as float
+// into out[b * (nt + 1) + n].
+template <int Q>
+__global__ void __launch_bounds__(TransformShape<Q>::kThreads) fk_transform(
+    FkGeom g, SeriesTab tab, long long g0, int P, int nt, const float4* __restrict__ U,
+    const float4* __restrict__ Ph, const float2* __restrict__ cosd, const float4* __restrict__ twM,
+    const float4* __restrict__ twN, const double* __restrict__ escale, float* __restrict__ out)
+{
+    constexpr int T = TransformShape<Q>::kThreads;
+    extern __shared__ float4 fk_sm[];
     __shared__ SeriesPos sp;
-    const int b = blockIdx.y;
-    if (b >= nb) return;
+    const int b = blockIdx.x, r = blockIdx.y;
     if (threadIdx.x == 0) sp = decode(tab, g0 + b);
     __syncthreads();
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const SeriesPos p = sp;
     const int M = g.nh;
-    if (k > M / 2) return;
-    cd* const row = spec + (size_t)b * M;
-    if (k < g.K || M - k < g.K) {
-        const SeriesPos p = sp;
-        cd xk = series_bin(g, tab, p, k, U, Ph, cosphi);
-        cd xm = series_bin(g, tab, p, M - k, U, Ph, cosphi);
-        if (k == 0) {
-            xk.y = 0.0;
-            xm.y = 0.0;
+    if (P == 1) {
+        // pairs (k, M - k): each spectral bin is formed once and feeds both folded bins
+        for (int k = threadIdx.x; k <= M / 2; k += T) {
+            if (k < g.K || M - k < g.K) {
+                df64::C xk = series_bin(g, tab, p, k, U, Ph, cosd);
+                df64::C xm = k == 0 ? df64::zero() : series_bin(g, tab, p, M - k, U, Ph, cosd);
+                if (k == 0) {
+                    xk.hi.y = 0.f;
+                    xk.lo.y = 0.f;
+                }
+                fk_sm[k] = df64::pack(fold_bin(xk, xm, __ldg(&twN[k])));
+                if (k > 0 && 2 * k < M) fk_sm[M - k] = df64::pack(fold_bin(xm, xk, __ldg(&twN[M - k])));
+            } else {
+                fk_sm[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (2 * k < M) fk_sm[M - k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
         }
-        row[k] = fold_bin(xk, xm, tw[k]);
-        if (k > 0 && 2 * k < M) row[M - k] = fold_bin(xm, xk, tw[M - k]);
     } else {
-        row[k] = mk(0.0, 0.0);
-        if (2 * k < M) row[M - k] = mk(0.0, 0.0);
+        for (int kp = threadIdx.x; kp < Q; kp += T) {
+            df64::C acc = df64::zero();
+            for (int j = 0; j < P; ++j) {
+                const int k = kp + Q * j;
+                if (!(k < g.K || M - k < g.K)) continue;
+                df64::C z = fold_at(g, tab, p, k, U, Ph, cosd, twN);
+                const long long e = ((long long)j * r * Q) % M;          // w_P^{jr} = w_M^{jrQ}
+                if (e) z = df64::cmul(z, df64::unpack(__ldg(&twM[e])));
+                acc = df64::cadd(acc, z);
+            }
+            if (r && kp) acc = df64::cmul(acc, df64::unpack(__ldg(&twM[(size_t)kp * r])));
+            fk_sm[kp] = df64::pack(acc);
+        }
+    }
+    __syncthreads();
+    int Ns = 1;
+    if constexpr ((TransformShape<Q>::kLog & 1) != 0) {
+        stockham_stage<Q, 2>(fk_sm, Ns, P, twM);
+        Ns = 2;
+    }
+    if constexpr (Q >= 4) {
+#pragma unroll 1
+        for (; Ns < Q; Ns *= 4) stockham_stage<Q, 4>(fk_sm, Ns, P, twM);
+    }
+    float* const o = out + (size_t)b * (nt + 1);
+    for (int mp = threadIdx.x; mp < Q; mp += T) {
+        const long long n0 = 2LL * ((long long)P * mp + r);
+        if (n0 > nt) continue;
+        const df64::C z = df64::unpack(fk_sm[mp]);
+        o[n0] = (float)(df64::re_double(z) * escale[n0]);
+        if (n0 + 1 <= nt) o[n0 + 1] = (float)(df64::im_double(z) * escale[n0 + 1]);
     }
 }
 
-// strips[s][q + per_s * n] = float(y[b][n] * escale[n]), n = 0..nt; 32 x 32 tiles through shared memory.
-__global__ void fk_epilogue(SeriesTab tab, long long g0, int nb, int N, int nt, const double* __restrict__ y,
-                            const double* __restrict__ escale)
+// strips[s][q + per_s * n] = y[b][n], n = 0..nt; 32 x 32 tiles through shared memory.
+__global__ void fk_epilogue(SeriesTab tab, long long g0, int nb, int nt, const float* __restrict__ y)
 {
-    __shared__ double tile[32][33];
+    __shared__ float tile[32][33];
     const int n0 = blockIdx.x * 32, b0 = blockIdx.y * 32;
     const int tx = threadIdx.x, ty = threadIdx.y;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         const int b = b0 + ty + 8 * r, n = n0 + tx;
-        if (b < nb && n <= nt) tile[ty + 8 * r][tx] = y[(size_t)b * N + n];
+        if (b < nb && n <= nt) tile[ty + 8 * r][tx] = y[(size_t)b * (nt + 1) + n];
     }
     __syncthreads();
     const int b = b0 + tx;
@@ -394,8 +530,32 @@ __global__ void fk_epilogue(SeriesTab tab, long long g0, int nb, int N, int nt, 
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         const int n = n0 + ty + 8 * r;
-        if (n <= nt) dst[per * n] = (float)(tile[tx][ty + 8 * r] * escale[n]);
+        if (n <= nt) dst[per * n] = tile[tx][ty + 8 * r];
     }
+}
+
+// Launches fk_transform for transform length Q (power of two, <= kMaxQ).
+constexpr int kMaxQ = 4096;
+
+template <int Q>
+cudaError_t launch_transform_q(int q, dim3 grid, cudaStream_t st, const FkGeom& g, const SeriesTab& tab,
+                               long long g0, int P, int nt, const float4* U, const float4* Ph, const float2* cosd,
+                               const float4* twM, const float4* twN, const double* esc, float* out)
+{
+    if constexpr (Q > 1) {
+        if (q < Q) return launch_transform_q<Q / 2>(q, grid, st, g, tab, g0, P, nt, U, Ph, cosd, twM, twN, esc, out);
+    }
+    const size_t smem = sizeof(float4) * (size_t)Q;
+    static bool configured = false;
+    if (!configured) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(fk_transform<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    fk_transform<Q><<<grid, TransformShape<Q>::kThreads, smem, st>>>(g, tab, g0, P, nt, U, Ph, cosd, twM, twN, esc,
+                                                                     out);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------- host side
@@ -511,43 +671,6 @@ struct DevBufs {
     }
 };
 
-// Batched half-length Z2Z inverse plans, one per (device, length, batch), kept for the life of
-// the process.  They own no work area: each call supplies its own (stream-ordered), so calls on
-// different streams may use one plan at the same time.
-struct Z2ZPlan {
-    cufftHandle h = 0;
-    size_t work = 0;
-};
-
-std::mutex g_plan_mu;
-std::map<std::tuple<int, int, int>, Z2ZPlan> g_plans;
-
-cufftResult z2z_plan(int m, int batch, Z2ZPlan& out)
-{
-    int dev = 0;
-    cudaGetDevice(&dev);
-    std::lock_guard<std::mutex> lock(g_plan_mu);
-    const auto key = std::make_tuple(dev, m, batch);
-    auto it = g_plans.find(key);
-    if (it != g_plans.end()) {
-        out = it->second;
-        return CUFFT_SUCCESS;
-    }
-    Z2ZPlan p;
-    cufftResult r = cufftCreate(&p.h);
-    if (r != CUFFT_SUCCESS) return r;
-    int nn = m;
-    if ((r = cufftSetAutoAllocation(p.h, 0)) != CUFFT_SUCCESS ||
-        (r = cufftMakePlanMany(p.h, 1, &nn, nullptr, 1, m, nullptr, 1, m, CUFFT_Z2Z, batch, &p.work)) !=
-            CUFFT_SUCCESS) {
-        cufftDestroy(p.h);
-        return r;
-    }
-    g_plans[key] = p;
-    out = p;
-    return CUFFT_SUCCESS;
-}
-
 }  // namespace
 
 size_t fk_strip_elems(int nx, int nz, int nbd, int k)
@@ -569,15 +692,6 @@ size_t fk_strip_elems(int nx, int nz, int nbd, int k)
             return e_ == cudaErrorMemoryAllocation ? FDFK_ENOMEM : FDFK_ECUDA;                   \
         }                                                                                        \
     } while (0)
-#define FFT_CK(call)                                                                             \
-    do {                                                                                         \
-        cufftResult r_ = (call);                                                                 \
-        if (r_ != CUFFT_SUCCESS) {                                                               \
-            err = std::string(#call) + ": cuFFT status " + std::to_string((int)r_);              \
-            return r_ == CUFFT_ALLOC_FAILED ? FDFK_ENOMEM : FDFK_ECUDA;                          \
-        }                                                                                        \
-    } while (0)
-
 int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std::string& err, long long* launches)
 {
     if (J.nx < 1 || J.nbd < 1 || J.nz <= J.nbd || J.npml < J.nbd || J.nt < 1 || !(J.dt > 0.0) || !(J.dx > 0.0) ||
@@ -604,8 +718,8 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
     FkGeom g{};
     long long N = 1;
     while (N < 2LL * (J.nt + 1)) N *= 2;
-    if (N > (1LL << 28)) {
-        err = "FK: nt too large";
+    if (N > (1LL << 23)) {   // the df64 twiddle tables hold N/2 entries
+        err = "FK: nt too large (at most 4194302 time steps)";
         return FDFK_EINVAL;
     }
     g.N = (int)N;
@@ -630,7 +744,7 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
         escale[n] = std::exp(g.alpha * t) / (double)N;
     }
 
-    // columns 1-nbd .. nx+nbd: cos(baz) and the horizontal delay D
+    // columns 1-nbd .. nx+nbd: cos(baz) (FP64, and split into a df64 pair) and the horizontal delay D
     const int NXb = J.nx + 2 * J.npml;
     double sum = 0.0;
     for (int i = 0; i < NXb; ++i) sum += J.bazs[i];
@@ -639,12 +753,14 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
     const double xcen = J.x0 + half;
     const double rref = half * std::fabs(cbar);
     const int ncol = J.nx + 2 * J.nbd;
-    std::vector<double> cosphi(ncol), D(ncol);
+    std::vector<double> D(ncol);
+    std::vector<float2> cosd(ncol);
     for (int c = 0; c < ncol; ++c) {
         const int cx = c + 1 - J.nbd;
-        cosphi[c] = std::cos(J.bazs[cx - 1 + J.npml]);
+        const double cp = std::cos(J.bazs[cx - 1 + J.npml]);
+        df64::split(cp, cosd[c].x, cosd[c].y);
         const double x = J.x0 + (cx - 1) * J.dx;
-        D[c] = J.rayp * (cosphi[c] * (x - xcen) - rref);
+        D[c] = J.rayp * (cp * (x - xcen) - rref);
     }
 
     // series table
@@ -684,13 +800,15 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
 
     DevBufs B(stream);
     FkLayer *d_lay0, *d_lay1;
-    double *d_w, *d_esc, *d_cos, *d_D;
-    cd *d_tw, *d_W, *d_amp0, *d_amp1, *d_U, *d_Ph, *d_spec;
+    double *d_w, *d_esc, *d_D;
+    float2* d_cos;
+    cd *d_tw, *d_W, *d_amp0, *d_amp1;
+    float4 *d_U, *d_Ph, *d_twM, *d_twN;
     FK_CK(B.alloc(&d_lay0, lay[0].size()));
     FK_CK(B.alloc(&d_lay1, lay[1].size()));
     FK_CK(B.alloc(&d_w, w.size()));
     FK_CK(B.alloc(&d_esc, escale.size()));
-    FK_CK(B.alloc(&d_cos, cosphi.size()));
+    FK_CK(B.alloc(&d_cos, cosd.size()));
     FK_CK(B.alloc(&d_D, D.size()));
     FK_CK(B.alloc(&d_tw, (size_t)g.N));
     FK_CK(B.alloc(&d_W, (size_t)g.K));
@@ -698,15 +816,18 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
     FK_CK(B.alloc(&d_amp1, (size_t)g.K * J.nlayer[1] * 4));
     FK_CK(B.alloc(&d_U, (size_t)2 * tab.nrow * g.K * 2));
     FK_CK(B.alloc(&d_Ph, (size_t)ncol * g.K));
+    FK_CK(B.alloc(&d_twM, (size_t)g.nh));
+    FK_CK(B.alloc(&d_twN, (size_t)g.nh));
     FK_CK(cudaMemcpyAsync(d_lay0, lay[0].data(), lay[0].size() * sizeof(FkLayer), cudaMemcpyHostToDevice, stream));
     FK_CK(cudaMemcpyAsync(d_lay1, lay[1].data(), lay[1].size() * sizeof(FkLayer), cudaMemcpyHostToDevice, stream));
     FK_CK(cudaMemcpyAsync(d_w, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
     FK_CK(cudaMemcpyAsync(d_esc, escale.data(), escale.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
-    FK_CK(cudaMemcpyAsync(d_cos, cosphi.data(), cosphi.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    FK_CK(cudaMemcpyAsync(d_cos, cosd.data(), cosd.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
     FK_CK(cudaMemcpyAsync(d_D, D.data(), D.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
 
     long long nl = 0;
     fk_twiddle<<<(g.N + 255) / 256, 256, 0, stream>>>(g.N, d_tw);
+    fk_df_twiddles<<<(g.nh + 255) / 256, 256, 0, stream>>>(g.nh, d_twM, d_twN);
     fk_source_dft<<<g.K, 256, 0, stream>>>(J.nt, g.N, d_w, d_tw, d_W);
     fk_layer_amps<<<(2 * g.K + 127) / 128, 128, 0, stream>>>(g, d_lay0, d_lay1, J.nlayer[0], J.nlayer[1],
                                                              J.p_wave ? 2 : 3, -1.0, J.z0 + (J.nz - 1) * J.dz,
@@ -721,36 +842,29 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
         const long long n = (long long)ncol * g.K;
         fk_column_phase<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(g, ncol, d_D, d_W, d_Ph);
     }
-    nl += 5;
+    nl += 6;
     FK_CK(cudaGetLastError());
 
-    // batches of series: the half-length complex transform runs in place, N doubles per series
-    const size_t per_series = (size_t)g.N * sizeof(double);
-    const size_t budget = (size_t)2 << 30;
+    // the transform: Q-point branches (Q <= kMaxQ, P = M / Q branches per series); batches of
+    // series sized so that their float output (nt + 1 samples each) stays within a fixed budget
+    const int M = g.nh;
+    const int Q = std::min(M, kMaxQ), P = M / Q;
+    const size_t per_series = (size_t)(J.nt + 1) * sizeof(float);
+    const size_t budget = (size_t)1 << 30;
     long long bmax = std::max<long long>(1, std::min<long long>(nseries, (long long)(budget / per_series)));
     if (const char* e = std::getenv("FDFK_FK_BATCH")) {   // series per batch (tuning and tests)
         const long long v = std::atoll(e);
         if (v > 0) bmax = std::min(bmax, v);
     }
-    const int nb_full = (int)std::min<long long>(bmax, 65535);
-    FK_CK(B.alloc(&d_spec, (size_t)nb_full * g.nh));
-    const int tail = (int)(nseries % nb_full);
-    Z2ZPlan plan_full, plan_tail;
-    FFT_CK(z2z_plan(g.nh, nb_full, plan_full));
-    if (tail && nseries > nb_full) FFT_CK(z2z_plan(g.nh, tail, plan_tail));
-    void* work = nullptr;
-    FK_CK(B.alloc(reinterpret_cast<char**>(&work), std::max(plan_full.work, plan_tail.work)));
-    for (long long g0 = 0; g0 < nseries; g0 += nb_full) {
-        const int nb = (int)std::min<long long>(nb_full, nseries - g0);
-        const dim3 ga((g.nh / 2 + 1 + 255) / 256, nb);
-        fk_assemble<<<ga, 256, 0, stream>>>(g, tab, g0, nb, d_U, d_Ph, d_cos, d_tw, d_spec);
-        const Z2ZPlan& pl = nb == nb_full ? plan_full : plan_tail;
-        FFT_CK(cufftSetWorkArea(pl.h, work));
-        FFT_CK(cufftSetStream(pl.h, stream));
-        FFT_CK(cufftExecZ2Z(pl.h, (cufftDoubleComplex*)d_spec, (cufftDoubleComplex*)d_spec, CUFFT_INVERSE));
+    bmax = std::min<long long>(bmax, 1 << 30);
+    float* d_out;
+    FK_CK(B.alloc(&d_out, (size_t)bmax * (J.nt + 1)));
+    for (long long g0 = 0; g0 < nseries; g0 += bmax) {
+        const int nb = (int)std::min<long long>(bmax, nseries - g0);
+        FK_CK(launch_transform_q<kMaxQ>(Q, dim3(nb, P), stream, g, tab, g0, P, J.nt, d_U, d_Ph, d_cos, d_twM,
+                                        d_twN, d_esc, d_out));
         const dim3 ge((J.nt + 1 + 31) / 32, (nb + 31) / 32);
-        fk_epilogue<<<ge, dim3(32, 8), 0, stream>>>(tab, g0, nb, g.N, J.nt, reinterpret_cast<const double*>(d_spec),
-                                                    d_esc);
+        fk_epilogue<<<ge, dim3(32, 8), 0, stream>>>(tab, g0, nb, J.nt, d_out);
         nl += 2;
         FK_CK(cudaGetLastError());
     }
