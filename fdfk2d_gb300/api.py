@@ -221,11 +221,13 @@ class Session:
     def advance(self, nsteps: int):
         _check(lib().fdfk_session_advance(self._h, C.c_int(nsteps)))
 
-    def advance_timed(self, nsteps: int):
-        """Advance with CUDA events around each kernel; returns (ms_interior, ms_edge, ms_total): the
-        summed times of the fast-path and tiled kernels and the time of all the steps, from one loop."""
+    def advance_timed(self, nsteps: int, sample_every: int = 1):
+        """Advance with CUDA events around the kernels of every sample_every-th step; returns
+        (ms_interior, ms_edge, ms_total): the mean time per launch of the fast-path and tiled
+        kernels over the sampled steps and the time of all the steps, from one loop."""
         ti, te, tt = C.c_float(), C.c_float(), C.c_float()
-        _check(lib().fdfk_session_advance_timed(self._h, C.c_int(nsteps), C.byref(ti), C.byref(te), C.byref(tt)))
+        _check(lib().fdfk_session_advance_timed(self._h, C.c_int(nsteps), C.c_int(sample_every), C.byref(ti),
+                                                C.byref(te), C.byref(tt)))
         return float(ti.value), float(te.value), float(tt.value)
 
     def cell_split(self):

@@ -506,9 +506,11 @@ int fdfk_session_advance(fdfk_session* s, int nsteps)
     return FDFK_OK;
 }
 
-int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, float* ms_edge, float* ms_total)
+int fdfk_session_advance_timed(fdfk_session* s, int nsteps, int sample_every, float* ms_interior, float* ms_edge,
+                               float* ms_total)
 {
     if (!s || !ms_interior || !ms_edge) return fail(FDFK_EINVAL, "NULL argument");
+    if (sample_every < 1) return fail(FDFK_EINVAL, "sample_every must be at least 1");
     if (s->batch) return fail(FDFK_ESTATE, "the session is a member of a batch; advance the batch");
     *ms_interior = 0.f;
     *ms_edge = 0.f;
@@ -539,20 +541,22 @@ int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, 
             s->istp += 1;
             s->isis += s->nstp;
         }
+        // the kernels of every sample_every-th step are bracketed by event pairs
+        const bool sampled = k % sample_every == 0;
         cudaEvent_t* e = &ev[(size_t)k * 4];
         cudaStream_t edge = two ? s->side : s->stream;
         if (two) {
             cudaEventRecord(s->fork, s->stream);
             cudaStreamWaitEvent(s->side, s->fork, 0);
         }
-        cudaEventRecord(e[2], edge);
+        if (sampled) cudaEventRecord(e[2], edge);
         int nl = 0;
         cudaError_t r = launch_edge(s, a, edge, &nl);
-        cudaEventRecord(e[3], edge);
+        if (sampled) cudaEventRecord(e[3], edge);
         if (r == cudaSuccess && two) {
             // e[0] .. e[1] brackets the fast-path kernel alone (the frame kernel runs before e[0])
-            r = launch_march_marked(a, s->march, s->stream, e[0]);
-            cudaEventRecord(e[1], s->stream);
+            r = launch_march_marked(a, s->march, s->stream, sampled ? e[0] : nullptr);
+            if (sampled) cudaEventRecord(e[1], s->stream);
             cudaEventRecord(s->join, s->side);
             cudaStreamWaitEvent(s->stream, s->join, 0);
         }
@@ -568,14 +572,16 @@ int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, 
         if (cudaEventElapsedTime(&t, t_begin, t_end) == cudaSuccess) *ms_total = t;
     }
     double ti = 0.0, te = 0.0;
-    for (int k = 0; k < nsteps; ++k) {
+    int ns = 0;
+    for (int k = 0; k < nsteps; k += sample_every) {
         float t = 0.f;
         if (two && cudaEventElapsedTime(&t, ev[(size_t)k * 4], ev[(size_t)k * 4 + 1]) == cudaSuccess) ti += t;
         if (cudaEventElapsedTime(&t, ev[(size_t)k * 4 + 2], ev[(size_t)k * 4 + 3]) == cudaSuccess) te += t;
+        ++ns;
     }
     cleanup();
-    *ms_interior = (float)ti;
-    *ms_edge = (float)te;
+    *ms_interior = (float)(ti / ns);
+    *ms_edge = (float)(te / ns);
     return FDFK_OK;
 }
 

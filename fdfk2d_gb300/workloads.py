@@ -221,3 +221,68 @@ def check_shapes(w, strips):
     shp = strip_shapes(p["nx"], p["nz"], p["nbd"], p["nt"])
     for k in STRIPS:
         assert strips[k].shape[:2] == shp[k][:2], k
+
+
+def config4_solves(n=96, seed=4):
+    """The uneven batch (config 4): n solves with grid sizes nx log-uniform in 500-6000 and nz
+    log-uniform in 250-2500, dx = dz uniform in 100-500 m, simulated length uniform in 20-120 s with
+    dt from the CFL limit of FD order 6 (0.9 of it) and nt = length / dt; a random two- to four-layer
+    crust/mantle model (crustal interfaces over a Moho at 30-55 km) with a 0-5 % Gaussian-smoothed
+    Vp/Vs perturbation (5 km correlation); P (0.04-0.08 s/km) or S (0.10-0.12 s/km) incidence, back-
+    azimuth uniform in 0-360 degrees, Ricker 0.5-1 Hz; 20-cell PML; receivers every 2 km at the
+    surface.  Each entry: a workload dict as config1/config2 make, plus its event and FK models."""
+    rng = np.random.default_rng(seed)
+    cfl6 = 0.5752                         # sqrt(2 / ((cx + cz) (sum |c2| + sum c2))) of order 6
+    out = []
+    for i in range(n):
+        nx = int(round(math.exp(rng.uniform(math.log(500), math.log(6000)))))
+        nz = int(round(math.exp(rng.uniform(math.log(250), math.log(2500)))))
+        h = float(np.float32(rng.uniform(100.0, 500.0)))
+        length = float(rng.uniform(20.0, 120.0))
+        nlayer = int(rng.integers(2, 5))
+        moho = float(rng.uniform(30e3, 55e3))
+        tops = [0.0] + sorted(float(t) for t in rng.uniform(2e3, moho - 2e3, nlayer - 2)) + [moho]
+        vps = list(np.linspace(5600.0, 6800.0, nlayer - 1) + rng.uniform(-200.0, 200.0, nlayer - 1)) + [8100.0]
+        vss = [v / 1.75 for v in vps[:-1]] + [4500.0]
+        pert_std = float(rng.uniform(0.0, 0.05))
+        npml = 20
+        NZ, NX = nz + npml, nx + 2 * npml
+        z = (np.arange(NZ) * h)[:, None]
+        vp = np.zeros((NZ, 1))
+        vs = np.zeros((NZ, 1))
+        for t, a, b in zip(tops, vps, vss):
+            vp = np.where(z >= t, a, vp)
+            vs = np.where(z >= t, b, vs)
+        vp = vp * np.ones((1, NX))
+        vs = vs * np.ones((1, NX))
+        if pert_std > 0.0:
+            pert = _smooth_noise(rng, NZ, NX, h, 5e3, pert_std)
+            vp = vp * (1.0 + pert)
+            vs = vs * (1.0 + pert)
+        vmax = float(vp.max())
+        dt = float(0.9 * cfl6 * h / vmax)
+        nt = int(math.ceil(length / dt))
+        p_wave = bool(rng.random() < 0.5)
+        lo, hi = (0.04, 0.08) if p_wave else (0.10, 0.12)
+        ev = dict(p_wave=p_wave, rayp=float(rng.uniform(lo, hi)) * 1e-3, baz=float(rng.uniform(0.0, 360.0)),
+                  f0=float(np.float32(rng.uniform(0.5, 1.0))))
+        nrcv = max(2, int((nx - 1) * h // 2000.0) + 1)
+        w = _base(f"config4 solve {i}: {nx}x{nz} @ {h:.0f} m, {nlayer} layers, {length:.0f} s", nx, nz, npml, h, dt,
+                  nt, nrcv, ev["rayp"] * 1e3, ev["f0"])
+        w["c"] = pack_c(vp, vs)
+        w["p"]["vpml"] = vmax
+        fkm = np.asfortranarray(np.stack([np.asarray(tops), np.asarray(vps), np.asarray(vss),
+                                          gardner(np.asarray(vps))]).astype(np.float32))
+        w["event"] = ev
+        w["fk_model"] = fkm
+        out.append(w)
+    return out
+
+
+def config4_inputs(w, ds=1e-3):
+    """FK arguments (params, bazs, fk_left, fk_right) of a config-4 solve (same 1-D model both sides)."""
+    p, ev = w["p"], w["event"]
+    fp = dict(nx=p["nx"], nz=p["nz"], npml=p["npml"], izt=1, nbd=p["nbd"], nt=p["nt"], src_type=ev["p_wave"],
+              x0=w["x0"], z0=w["z0"], dx=p["dx"], dz=p["dz"], dt=p["dt"], ds=ds, f0=ev["f0"], rayp=ev["rayp"])
+    bazs = np.full(p["nx"] + 2 * p["npml"], np.deg2rad(ev["baz"]))
+    return fp, bazs, w["fk_model"], w["fk_model"]

@@ -94,14 +94,16 @@ int fdfk_session_set_receivers(fdfk_session* s, int nrcv, const float* rx, const
 int fdfk_session_advance(fdfk_session* s, int nsteps);
 
 /*
- * fdfk_session_advance with a CUDA-event pair around every kernel launch (on
- * the stream that launches it), then a synchronize: *ms_interior is the summed
- * time of the interior fast-path kernel, *ms_edge that of the tiled kernel
+ * fdfk_session_advance with a CUDA-event pair around each kernel launch of
+ * every sample_every-th step (on the stream that launches it), then a
+ * synchronize: *ms_interior is the mean time per launch of the interior
+ * fast-path kernel over the sampled steps, *ms_edge that of the tiled kernel
  * (top rows, absorbing layers, receivers), and *ms_total (if not NULL) the
  * time of all nsteps steps between two events on the session's stream, so the
  * kernels' times and the steps' time come from the same loop.  Measurement only.
  */
-int fdfk_session_advance_timed(fdfk_session* s, int nsteps, float* ms_interior, float* ms_edge, float* ms_total);
+int fdfk_session_advance_timed(fdfk_session* s, int nsteps, int sample_every, float* ms_interior, float* ms_edge,
+                               float* ms_total);
 
 /* Cells per step handled by the interior fast path and by the tiled kernel. */
 int fdfk_session_interior_cells(const fdfk_session* s, long long* interior, long long* edge);

@@ -94,3 +94,38 @@ def test_request_larger_than_budget_is_refused(F):
         with pytest.raises(F.FDFKError) as e:
             srv.submit(**r)
         assert e.value.code == -1
+
+
+def test_served_config3_traces_vs_fp64_oracle(F, oracle_lib):
+    """A stream of config-3 requests (events on the 801 x 401 two-layer model, 4001 steps, P and S
+    incidence, back-azimuths 0-360, 0.5-1 Hz) served with staggered arrivals; 8 requests chosen by a
+    seeded draw are checked trace by trace against the FP64 GPU oracle fed the FP64 FK restatement:
+    relative L2 of every trace at most 1e-4."""
+    import fk_oracle
+    from fdfk2d_gb300 import workloads as WL
+    w = WL.config1()
+    p = w["p"]
+    events = WL.config3_events(24, seed=23)
+    pick = sorted(np.random.default_rng(5).choice(len(events), 8, replace=False).tolist())
+    ids = []
+    with F.Server(3, budget_bytes=40 << 30, chunk=64) as srv:
+        for i, ev in enumerate(events):
+            fp, bazs, fl, fr = WL.event_inputs(w, ev)
+            ids.append(srv.submit(p, w["c"], fp, bazs, fl, fr, w["rx"], w["rz"], w["x0"], w["z0"], 1, p["nt"]))
+            if i % 3 == 2:                                  # later requests arrive while earlier ones run
+                srv.pump()
+        while srv.pump() > 0:
+            pass
+        got = {i: tuple(np.array(a) for a in srv.result(ids[i])) for i in pick}
+    worst = 0.0
+    for i in pick:
+        fp, bazs, fl, fr = WL.event_inputs(w, events[i])
+        strips = fk_oracle.background_device(fp, bazs, fl, fr, x0=w["x0"], z0=w["z0"])
+        ox, oz = oracle_lib.simulate64_gpu(dict(p, izt=1), strips, w["c"], w["rx"], w["rz"], w["x0"], w["z0"], 1,
+                                           p["nt"])
+        del strips
+        for g, o in zip(got[i], (ox, oz)):
+            e = np.linalg.norm(g.astype(np.float64) - o, axis=0) / np.linalg.norm(o, axis=0)
+            worst = max(worst, float(e.max()))
+    print(f"\nserved config-3 requests {pick}: worst per-trace relative L2 vs FP64 oracle {worst:.3e}")
+    assert worst <= 1e-4
