@@ -151,6 +151,7 @@ int rebuild(fdfk_batch* b)
         a.nsamp = s->nsis + 1;
         a.x0 = s->x0; a.z0 = s->z0;
         a.rx = s->rx; a.rz = s->rz;
+        a.rsite = s->rsite; a.rw = s->rw;
         a.seisx = s->seisx; a.seisz = s->seisz;
         args[i] = a;
         MarchArgs m = s->march;

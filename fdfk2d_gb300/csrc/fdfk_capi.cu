@@ -144,7 +144,7 @@ void free_session(fdfk_session* s)
     for (int k = 0; k < 12; ++k) cudaFree(s->bp[k]);
     cudaFree(s->dampx); cudaFree(s->dampz);
     for (int k = 0; k < NSTRIP; ++k) cudaFree(s->strip[k]);
-    cudaFree(s->rx); cudaFree(s->rz); cudaFree(s->seisx); cudaFree(s->seisz);
+    cudaFree(s->rx); cudaFree(s->rz); cudaFree(s->rsite); cudaFree(s->rw); cudaFree(s->seisx); cudaFree(s->seisz);
     delete s;
 }
 
@@ -434,8 +434,10 @@ int fdfk_session_set_receivers(fdfk_session* s, int nrcv, const float* rx, const
     for (int r = 0; r < nrcv; ++r)
         if (rx[r] < x0 || rx[r] > xmax || rz[r] < z0 || rz[r] > zmax)
             return fail(FDFK_EINVAL, "receiver " + std::to_string(r + 1) + " lies outside the model");
-    cudaFree(s->rx); cudaFree(s->rz); cudaFree(s->seisx); cudaFree(s->seisz);
+    cudaFree(s->rx); cudaFree(s->rz); cudaFree(s->rsite); cudaFree(s->rw); cudaFree(s->seisx); cudaFree(s->seisz);
     s->rx = s->rz = s->seisx = s->seisz = nullptr;
+    s->rsite = nullptr;
+    s->rw = nullptr;
     s->nrcv = nrcv; s->nstp = nstp; s->nsis = nsis; s->x0 = x0; s->z0 = z0;
     if (nrcv > 0) {
         const size_t ns = (size_t)(nsis + 1) * nrcv;
@@ -447,6 +449,10 @@ int fdfk_session_set_receivers(fdfk_session* s, int nrcv, const float* rx, const
         CK(cudaMemcpyAsync(s->rz, rz, nrcv * sizeof(float), cudaMemcpyHostToDevice, s->stream));
         CK(cudaMemsetAsync(s->seisx, 0, ns * sizeof(float), s->stream));
         CK(cudaMemsetAsync(s->seisz, 0, ns * sizeof(float), s->stream));
+        CK(cudaMalloc((void**)&s->rsite, nrcv * sizeof(int4)));
+        CK(cudaMalloc((void**)&s->rw, (size_t)nrcv * 49 * sizeof(double)));
+        CK(fdfk::launch_receiver_sites(s->base, nrcv, x0, z0, s->rx, s->rz, s->rsite, s->rw, s->stream));
+        fdfk::count_launches(1);
         // no wait: copies from pageable memory are staged before the call returns, and everything
         // that reads these arrays is ordered after them on the session's stream (a batch waits for
         // the stream when the session joins), so an FK background still running is not waited for
@@ -478,6 +484,7 @@ int fdfk_session_advance(fdfk_session* s, int nsteps)
             a.nsamp = s->nsis + 1;
             a.x0 = s->x0; a.z0 = s->z0;
             a.rx = s->rx; a.rz = s->rz;
+            a.rsite = s->rsite; a.rw = s->rw;
             a.seisx = s->seisx; a.seisz = s->seisz;
             s->istp += 1;
             s->isis += s->nstp;
@@ -538,6 +545,7 @@ int fdfk_session_advance_timed(fdfk_session* s, int nsteps, int sample_every, fl
         if (s->nrcv > 0 && s->isis == it && s->istp <= s->nsis) {
             a.nrcv = s->nrcv; a.sample_index = s->istp; a.nsamp = s->nsis + 1;
             a.x0 = s->x0; a.z0 = s->z0; a.rx = s->rx; a.rz = s->rz; a.seisx = s->seisx; a.seisz = s->seisz;
+            a.rsite = s->rsite; a.rw = s->rw;
             s->istp += 1;
             s->isis += s->nstp;
         }

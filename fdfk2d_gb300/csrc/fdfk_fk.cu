@@ -448,7 +448,7 @@ template <int Q>
 __global__ void __launch_bounds__(TransformShape<Q>::kThreads) fk_transform(
     FkGeom g, SeriesTab tab, long long g0, int P, int nt, const float4* __restrict__ U,
     const float4* __restrict__ Ph, const float2* __restrict__ cosd, const float4* __restrict__ twM,
-    const float4* __restrict__ twN, const double* __restrict__ escale, float* __restrict__ out)
+    const float4* __restrict__ twN, const float2* __restrict__ escale, float* __restrict__ out)
 {
     constexpr int T = TransformShape<Q>::kThreads;
     extern __shared__ float4 fk_sm[];
@@ -504,9 +504,19 @@ __global__ void __launch_bounds__(TransformShape<Q>::kThreads) fk_transform(
     for (int mp = threadIdx.x; mp < Q; mp += T) {
         const long long n0 = 2LL * ((long long)P * mp + r);
         if (n0 > nt) continue;
+        // x[n0] = Re z, x[n0+1] = Im z, each times its df64 scale exp(alpha t)/N (table padded to nt + 2);
+        // the float nearest to the df64 product is the rounded sum of its two parts (no FP64 here: on
+        // this GPU a few FP64 operations per output cost as much as the whole transform)
         const df64::C z = df64::unpack(fk_sm[mp]);
-        o[n0] = (float)(df64::re_double(z) * escale[n0]);
-        if (n0 + 1 <= nt) o[n0 + 1] = (float)(df64::im_double(z) * escale[n0 + 1]);
+        const float2 e0 = __ldg(&escale[n0]), e1 = __ldg(&escale[n0 + 1]);
+        const float2 eh = df64::f2(e0.x, e1.x), el = df64::f2(e0.y, e1.y);
+        const float2 ph = df64::mul(z.hi, eh);
+        float2 pe = df64::fma(z.hi, eh, df64::f2(-ph.x, -ph.y));
+        pe = df64::fma(z.hi, el, pe);
+        pe = df64::fma(z.lo, eh, pe);
+        const float2 x = df64::add(ph, pe);
+        o[n0] = x.x;
+        if (n0 + 1 <= nt) o[n0 + 1] = x.y;
     }
 }
 
@@ -540,7 +550,7 @@ constexpr int kMaxQ = 4096;
 template <int Q>
 cudaError_t launch_transform_q(int q, dim3 grid, cudaStream_t st, const FkGeom& g, const SeriesTab& tab,
                                long long g0, int P, int nt, const float4* U, const float4* Ph, const float2* cosd,
-                               const float4* twM, const float4* twN, const double* esc, float* out)
+                               const float4* twM, const float4* twN, const float2* esc, float* out)
 {
     if constexpr (Q > 1) {
         if (q < Q) return launch_transform_q<Q / 2>(q, grid, st, g, tab, g0, P, nt, U, Ph, cosd, twM, twN, esc, out);
@@ -737,11 +747,13 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
 
     // damped, delayed Ricker samples and the output scale exp(alpha t_n) / N
     std::vector<double> w(J.nt + 1), escale(J.nt + 1);
+    std::vector<float2> escf(J.nt + 2, float2{0.f, 0.f});   // df64 pairs, one spare entry
     for (int n = 0; n <= J.nt; ++n) {
         const double t = n * J.dt;
         const double a = (kPi * J.f0 * (t - 1.25 / J.f0)) * (kPi * J.f0 * (t - 1.25 / J.f0));
         w[n] = J.ds * (1.0 - 2.0 * a) * std::exp(-a) * std::exp(-g.alpha * t);
         escale[n] = std::exp(g.alpha * t) / (double)N;
+        df64::split(escale[n], escf[n].x, escf[n].y);
     }
 
     // columns 1-nbd .. nx+nbd: cos(baz) (FP64, and split into a df64 pair) and the horizontal delay D
@@ -800,14 +812,15 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
 
     DevBufs B(stream);
     FkLayer *d_lay0, *d_lay1;
-    double *d_w, *d_esc, *d_D;
+    double *d_w, *d_D;
+    float2* d_esc;
     float2* d_cos;
     cd *d_tw, *d_W, *d_amp0, *d_amp1;
     float4 *d_U, *d_Ph, *d_twM, *d_twN;
     FK_CK(B.alloc(&d_lay0, lay[0].size()));
     FK_CK(B.alloc(&d_lay1, lay[1].size()));
     FK_CK(B.alloc(&d_w, w.size()));
-    FK_CK(B.alloc(&d_esc, escale.size()));
+    FK_CK(B.alloc(&d_esc, escf.size()));
     FK_CK(B.alloc(&d_cos, cosd.size()));
     FK_CK(B.alloc(&d_D, D.size()));
     FK_CK(B.alloc(&d_tw, (size_t)g.N));
@@ -821,7 +834,7 @@ int fk_background(const FkJob& J, float* const dst[12], cudaStream_t stream, std
     FK_CK(cudaMemcpyAsync(d_lay0, lay[0].data(), lay[0].size() * sizeof(FkLayer), cudaMemcpyHostToDevice, stream));
     FK_CK(cudaMemcpyAsync(d_lay1, lay[1].data(), lay[1].size() * sizeof(FkLayer), cudaMemcpyHostToDevice, stream));
     FK_CK(cudaMemcpyAsync(d_w, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
-    FK_CK(cudaMemcpyAsync(d_esc, escale.data(), escale.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    FK_CK(cudaMemcpyAsync(d_esc, escf.data(), escf.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
     FK_CK(cudaMemcpyAsync(d_cos, cosd.data(), cosd.size() * sizeof(float2), cudaMemcpyHostToDevice, stream));
     FK_CK(cudaMemcpyAsync(d_D, D.data(), D.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
 

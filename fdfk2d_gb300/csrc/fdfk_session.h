@@ -36,6 +36,8 @@ struct fdfk_session {
     float x0 = 0.f, z0 = 0.f;
     float* rx = nullptr;
     float* rz = nullptr;
+    int4* rsite = nullptr;
+    double* rw = nullptr;
     float* seisx = nullptr;
     float* seisz = nullptr;
     fdfk::StepArgs base{};

@@ -197,8 +197,49 @@ __device__ __forceinline__ double delta_weight(double x)
     return 0.0;
 }
 
-// One warp per receiver: the lanes share the (at most) 7 x 7 grid points, each forms its weight
-// and product in FP64, and a shuffle reduction sums them (FP64).
+// The grid point (irx, irz) a receiver's 7 x 7 neighbourhood is centred on, which points of it lie
+// in the model (bit q of the masks: point q = 7 * (column offset + 3) + row offset + 3) and each
+// point's FP64 weight; formed once when the receivers are set.  Block r, 64 threads: thread q < 49
+// forms point q.
+__global__ void receiver_sites_kernel(int nrcv, int nx, int nz, int npml, float dx, float dz, float x0, float z0,
+                                      const float* __restrict__ rxs, const float* __restrict__ rzs,
+                                      int4* __restrict__ site, double* __restrict__ wout)
+{
+    const int r = blockIdx.x, q = threadIdx.x;
+    if (r >= nrcv) return;
+    const float rx = rxs[r], rz = rzs[r];
+    const int irx = (int)floorf((rx - x0) / dx) + 1;
+    const int irz = (int)floorf((rz - z0) / dz) + 1;
+    const int xlo = max(1 - npml, irx - 3), xhi = min(nx + npml, irx + 3);
+    const int zlo = max(1, irz - 3), zhi = min(nz + npml, irz + 3);
+    const int ix = irx - 3 + q / 7, iz = irz - 3 + q % 7;
+    const bool in = q < 49 && ix >= xlo && ix <= xhi && iz >= zlo && iz <= zhi;
+    double w = 0.0;
+    if (in) {
+        const double x = fabs((double)__fadd_rn(x0, __fmul_rn((float)(ix - 1), dx)) - (double)rx) / (double)dx;
+        const double z = fabs((double)__fadd_rn(z0, __fmul_rn((float)(iz - 1), dz)) - (double)rz) / (double)dz;
+        w = delta_weight(x) * delta_weight(z);
+    }
+    if (q < 49) wout[(size_t)r * 49 + q] = w;
+    const unsigned m = __ballot_sync(0xffffffffu, in);
+    if ((q & 31) == 0) {
+        int* s = reinterpret_cast<int*>(site + r);
+        if (q == 0) { s[0] = irx; s[1] = irz; s[2] = (int)m; }
+        else s[3] = (int)m;
+    }
+}
+
+cudaError_t launch_receiver_sites(const StepArgs& a, int nrcv, float x0, float z0, const float* rx,
+                                  const float* rz, int4* site, double* w, cudaStream_t s)
+{
+    if (nrcv <= 0) return cudaSuccess;
+    receiver_sites_kernel<<<nrcv, 64, 0, s>>>(nrcv, a.nx, a.nz, a.npml, a.dx, a.dz, x0, z0, rx, rz, site, w);
+    return cudaGetLastError();
+}
+
+// One warp per receiver: the lanes share the (at most) 7 x 7 grid points, each adds its points'
+// weighted displacements in FP64 (weights formed by receiver_sites_kernel), and a shuffle reduction
+// sums them (FP64).
 __device__ void sample_receivers(const StepArgs& a, int blk)
 {
     const int lane = threadIdx.x & 31;
@@ -206,21 +247,16 @@ __device__ void sample_receivers(const StepArgs& a, int blk)
     if (r >= a.nrcv) return;
     const float* ux = a.ux[a.cur];
     const float* uz = a.uz[a.cur];
-    const float rx = a.rx[r], rz = a.rz[r];
-    const int irx = (int)floorf((rx - a.x0) / a.dx) + 1;
-    const int irz = (int)floorf((rz - a.z0) / a.dz) + 1;
-    const int xlo = max(1 - a.npml, irx - 3), xhi = min(a.nx + a.npml, irx + 3);
-    const int zlo = max(1, irz - 3), zhi = min(a.nz + a.npml, irz + 3);
+    const int4 st = a.rsite[r];
+    const double* w = a.rw + (size_t)r * 49;
     double sx = 0.0, sz = 0.0;
     for (int q = lane; q < 49; q += 32) {
-        const int ix = irx - 3 + q / 7, iz = irz - 3 + q % 7;
-        if (ix < xlo || ix > xhi || iz < zlo || iz > zhi) continue;
-        const double x = fabs((double)__fadd_rn(a.x0, __fmul_rn((float)(ix - 1), a.dx)) - (double)rx) / (double)a.dx;
-        const double z = fabs((double)__fadd_rn(a.z0, __fmul_rn((float)(iz - 1), a.dz)) - (double)rz) / (double)a.dz;
-        const double w = delta_weight(x) * delta_weight(z);
+        if ((((unsigned)(q < 32 ? st.z : st.w) >> (q & 31)) & 1u) == 0u) continue;
+        const int ix = st.x - 3 + q / 7, iz = st.y - 3 + q % 7;
         const size_t g = gidx(a, iz, ix);
-        sx += w * (double)ux[g];
-        sz += w * (double)uz[g];
+        const double wq = w[q];
+        sx += wq * (double)ux[g];
+        sz += wq * (double)uz[g];
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {

@@ -80,6 +80,8 @@ struct StepArgs {
     float x0, z0;
     const float* __restrict__ rx;
     const float* __restrict__ rz;
+    const int4* __restrict__ rsite;     // per receiver: grid point (ix, iz), masks of points 0..31, 32..48
+    const double* __restrict__ rw;      // per receiver: FP64 weights of its 7 x 7 points
     float* seisx;
     float* seisz;
     int it;                    // time index of the background strips
@@ -102,6 +104,10 @@ void plan_tiles(StepArgs& a, bool band_top, int pml_run = kPmlRun);
 size_t step_smem_for(const StepArgs& a);
 // Receiver-sampling blocks a tiled launch appends for nrcv receivers.
 int sample_blocks(int nrcv);
+// Sites and weights of nrcv receivers at (rx, rz) (device arrays) for a's grid (nx, nz, npml, dx,
+// dz) with origin (x0, z0): site[nrcv], w[49 * nrcv].
+cudaError_t launch_receiver_sites(const StepArgs& a, int nrcv, float x0, float z0, const float* rx,
+                                  const float* rz, int4* site, double* w, cudaStream_t s);
 
 // Device-side per-member state of a batch (advanced by fdfk_batch_bump before every step).
 struct BatchDyn {
