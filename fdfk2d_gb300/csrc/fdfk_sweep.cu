@@ -31,13 +31,16 @@ __constant__ float c_coll[kMaxOrder + 1][kMaxOrder + 1];  // [n][j]: fd_coef1(j,
 // that order), and the split-field update's F2 and F3 of each component.
 enum { kFsA, kFsQx, kFsB, kFsQz, kFsF2x, kFsF3x, kFsF2z, kFsF3z, kFsTerms };
 
-// Shared-memory layout of a TZ x TX tile (z fastest) for stencil half-order NO.
+// Shared-memory layout of a TZ x TX tile (z fastest) for stencil half-order NO.  The cells of a
+// tile are handled in pairs of rows (z, z+1), z even, so every array has an even column stride
+// and an even row origin: the two rows of a pair are one aligned 8-byte access.
 struct TileDims {
     int TZ, TX;
-    int H;          // reach of dxx / dzz
-    int UZ, UX;     // u tile
-    int MZ, MX;     // material tile
-    int XW, ZW;     // extents of the x- / z-consumed arrays
+    int TZe;        // TZ rounded up to even (rows TZ..TZe-1 are computed, never stored)
+    int UZ, UX;     // u tile: rows -OU .. TZe+OU-1 (OU = 2 NO), columns -H .. TX+H-1 (H = 2 NO - 1)
+    int MZ, MX;     // material tile: rows -OM .. TZe+OM-1 (OM = NO rounded up to even), columns -NO .. TX+NO-1
+    int ZW;         // rows of the z-consumed arrays: -OM .. TZe+OM-1 (columns 0..TX-1)
+    int XW;         // columns of the x-consumed arrays: -NO .. TX+NO-1 (rows 0..TZe-1)
     int U, M, AX, AZ;
     int FS;         // free-surface terms of row 1 (kFsTerms per column)
     int total;      // floats
@@ -46,15 +49,16 @@ struct TileDims {
 __host__ __device__ __forceinline__ TileDims tile_dims(int NO, int TZ, int TX)
 {
     TileDims t;
+    const int H = 2 * NO - 1, OU = 2 * NO, OM = NO + (NO & 1);
     t.TZ = TZ; t.TX = TX;
-    t.H = 2 * NO - 1;
-    t.UZ = TZ + 2 * t.H; t.UX = TX + 2 * t.H;
-    t.MZ = TZ + 2 * NO; t.MX = TX + 2 * NO;
-    t.XW = TX + 2 * NO; t.ZW = TZ + 2 * NO;
+    t.TZe = (TZ + 1) & ~1;
+    t.UZ = t.TZe + 2 * OU; t.UX = TX + 2 * H;
+    t.MZ = t.TZe + 2 * OM; t.MX = TX + 2 * NO;
+    t.ZW = t.TZe + 2 * OM; t.XW = TX + 2 * NO;
     t.U = t.UZ * t.UX; t.M = t.MZ * t.MX;
-    t.AX = TZ * t.XW; t.AZ = t.ZW * TX;
+    t.AX = t.TZe * t.XW; t.AZ = t.ZW * TX;
     t.FS = kFsTerms * TX;
-    t.total = 2 * t.U + 4 * t.M + 4 * t.AX + 4 * t.AZ + t.FS;
+    t.total = 2 * t.U + 4 * t.M + 4 * t.AX + 4 * t.AZ + ((t.FS + 1) & ~1);
     return t;
 }
 
@@ -73,11 +77,30 @@ __device__ __forceinline__ float fast_rcp(float x)
     return r;
 }
 
+// (x / n, x % n) for 0 <= x < 2^20 and 1 <= n < 2^20: a single-precision reciprocal estimate is
+// within one of the quotient, and one correction makes it exact (cheaper than the integer
+// division sequence for a divisor known only at run time).
+__device__ __forceinline__ void divmod_small(int x, int n, int& q, int& r)
+{
+    q = __float2int_rz(__fmul_rn(__int2float_rn(x), fast_rcp(__int2float_rn(n))));
+    r = x - q * n;
+    if (r < 0) {
+        --q;
+        r += n;
+    } else if (r >= n) {
+        ++q;
+        r -= n;
+    }
+}
+
 // (i % n, i / n) along i = i0, i0 + step, ... without a division per step.
 struct Walk {
     int r, q, dr, dq, n;
-    __device__ __forceinline__ Walk(int i0, int n_, int step)
-        : r(i0 % n_), q(i0 / n_), dr(step % n_), dq(step / n_), n(n_) {}
+    __device__ __forceinline__ Walk(int i0, int n_, int step) : n(n_)
+    {
+        divmod_small(i0, n_, q, r);
+        divmod_small(step, n_, dq, dr);
+    }
     __device__ __forceinline__ void next()
     {
         r += dr;
@@ -128,27 +151,28 @@ __device__ __forceinline__ const float* outer_bg_ptr(const StepArgs& a, int iz, 
     return nullptr;
 }
 
-// Address of the background at (iz, ix) on the inner strips (Omega_I), as outer_bg_ptr.
-__device__ __forceinline__ const float* inner_bg_ptr(const StepArgs& a, int iz, int ix, const float*& pz)
+// One background strip as a rectangle of the grid: rows zr0..zr1, columns xr0..xr1, stored as
+// strip[(iz - zr0) + rows * ((ix - xr0) + cols * it)] (time slowest).  inner: the strips inside
+// the regular domain (Omega_I, removed from the absorbing layers' operator field), else the outer
+// strips (Omega_II, added to the regular field); k = 0 left, 1 right, 2 bottom.
+struct StripRect {
+    int zr0, zr1, xr0, xr1, rows, cols, sx, sz;
+};
+
+__device__ __forceinline__ StripRect strip_rect(const StepArgs& a, bool inner, int k)
 {
-    const int nx = a.nx, nz = a.nz, nbd = a.nbd, it = a.it;
-    if (ix < 1 || ix > nx || iz < 1 || iz > nz) return nullptr;
-    if (iz <= nz - nbd) {
-        if (ix <= nbd) {
-            const size_t o = (size_t)(iz - 1) + (size_t)(nz - nbd) * ((size_t)(ix - 1) + (size_t)nbd * it);
-            pz = a.strip[UZL_REG] + o;
-            return a.strip[UXL_REG] + o;
-        }
-        if (ix >= nx - nbd + 1) {
-            const size_t o = (size_t)(iz - 1) + (size_t)(nz - nbd) * ((size_t)(ix - (nx - nbd + 1)) + (size_t)nbd * it);
-            pz = a.strip[UZR_REG] + o;
-            return a.strip[UXR_REG] + o;
-        }
-        return nullptr;
+    const int nx = a.nx, nz = a.nz, nbd = a.nbd;
+    StripRect r;
+    if (inner) {
+        if (k == 0) r = {1, nz - nbd, 1, nbd, nz - nbd, nbd, UXL_REG, UZL_REG};
+        else if (k == 1) r = {1, nz - nbd, nx - nbd + 1, nx, nz - nbd, nbd, UXR_REG, UZR_REG};
+        else r = {nz - nbd + 1, nz, 1, nx, nbd, nx, UXB_REG, UZB_REG};
+    } else {
+        if (k == 0) r = {1, nz, 1 - nbd, 0, nz, nbd, UXL_PML, UZL_PML};
+        else if (k == 1) r = {1, nz, nx + 1, nx + nbd, nz, nbd, UXR_PML, UZR_PML};
+        else r = {nz + 1, nz + nbd, 1 - nbd, nx + nbd, nbd, nx + 2 * nbd, UXB_PML, UZB_PML};
     }
-    const size_t o = (size_t)(iz - (nz - nbd + 1)) + (size_t)nbd * ((size_t)(ix - 1) + (size_t)nx * it);
-    pz = a.strip[UZB_REG] + o;
-    return a.strip[UXB_REG] + o;
+    return r;
 }
 
 __device__ __forceinline__ Rect decode_tile(const StepArgs& a, int b)
@@ -159,7 +183,9 @@ __device__ __forceinline__ Rect decode_tile(const StepArgs& a, int b)
     if (b < ni) {
         r.side = 0;
         r.cls = 0;
-        r.z0 = 1 + (b % a.tiles_int_z) * a.tdz[0]; r.x0 = 1 + (b / a.tiles_int_z) * a.tdx[0];
+        int q, m;
+        divmod_small(b, a.tiles_int_z, q, m);
+        r.z0 = 1 + m * a.tdz[0]; r.x0 = 1 + q * a.tdx[0];
         r.zlo = 1; r.zhi = a.int_rows; r.xlo = 1; r.xhi = a.nx;
         return r;
     }
@@ -172,14 +198,18 @@ __device__ __forceinline__ Rect decode_tile(const StepArgs& a, int b)
         r.zlo = 1; r.zhi = a.nz;
         r.xlo = right ? a.nx + 1 : 1 - a.npml;
         r.xhi = right ? a.nx + a.npml : 0;
-        r.z0 = 1 + (b % a.tiles_l_z) * a.tdz[1]; r.x0 = r.xlo + (b / a.tiles_l_z) * a.tdx[1];
+        int q, m;
+        divmod_small(b, a.tiles_l_z, q, m);
+        r.z0 = 1 + m * a.tdz[1]; r.x0 = r.xlo + q * a.tdx[1];
         return r;
     }
     b -= 2 * nl;
     r.side = 3;
     r.cls = 2;
     r.zlo = a.nz + 1; r.zhi = a.nz + a.npml; r.xlo = 1 - a.npml; r.xhi = a.nx + a.npml;
-    r.z0 = r.zlo + (b % a.tiles_b_z) * a.tdz[2]; r.x0 = r.xlo + (b / a.tiles_b_z) * a.tdx[2];
+    int q, m;
+    divmod_small(b, a.tiles_b_z, q, m);
+    r.z0 = r.zlo + m * a.tdz[2]; r.x0 = r.xlo + q * a.tdx[2];
     return r;
 }
 
@@ -273,20 +303,52 @@ __device__ void sample_receivers(const StepArgs& a, int blk)
 // ---------------------------------------------------------------------------
 // The step kernel.
 // ---------------------------------------------------------------------------
+// Every phase works on pairs of rows (z, z+1) of one column, z even within the tile.  The two
+// rows go through the same operations, so each stencil tap and product is one packed FP32x2
+// instruction, rounded per row exactly as the scalar fmaf / __fadd_rn / __fmul_rn, and each
+// shared-memory operand of the pair one aligned 8-byte access.  All arithmetic is written with
+// explicit rounding: a cell's result is the same whichever row of a pair it is, whatever the
+// tile shape, and in the single-solve and batched kernels alike.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 f2s(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 psub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void sts2(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+
+// N consecutive rows of a z-fastest shared array from p (8-byte aligned): N/2 pair loads and, for
+// odd N, one scalar load.
+template <int N>
+__device__ __forceinline__ void load_rows(const float* p, float (&w)[N])
+{
+#pragma unroll
+    for (int i = 0; i + 1 < N; i += 2) {
+        const float2 t = lds2(p + i);
+        w[i] = t.x;
+        w[i + 1] = t.y;
+    }
+    if constexpr ((N & 1) != 0) w[N - 1] = p[N - 1];
+}
+
 // Block `blk` of one solve's tiled launch: a tile of the top band, an absorbing layer, or (past
 // n_tiles) a block of receivers.
 template <int NO>
 __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
 {
     constexpr int H = 2 * NO - 1;
-    extern __shared__ float sm[];
+    constexpr int OU = 2 * NO;              // row origin of the u tile (even)
+    constexpr int OM = NO + (NO & 1);       // row origin of the material tile and the z-consumed arrays
+    constexpr int NWIN = OM + NO + 2;       // rows z-OM .. z+1+NO: the z-stencil window of a pair
+    extern __shared__ __align__(16) float sm[];
     if (blk >= a.n_tiles) {
         sample_receivers(a, blk - a.n_tiles);
         return;
     }
     const Rect R = decode_tile(a, blk);
     const TileDims T = tile_dims(NO, a.tdz[R.cls], a.tdx[R.cls]);
-    const int TZ = T.TZ, TX = T.TX;
+    const int TZ = T.TZ, TX = T.TX, TZe = T.TZe;
     const bool pml = R.side != 0;
     const int tid = threadIdx.x;
     const int nx = a.nx, nz = a.nz, npml = a.npml;
@@ -308,81 +370,107 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
     float* v3 = v2 + T.AZ;     // lam * Dx(ux)/dx                 (dxz(lam ux))
     float* sFS = v3 + T.AZ;    // free-surface terms of row 1       [term][x]
 
+#define SU(arr, z, x) ((arr) + ((x) + H) * T.UZ + ((z) + OU))
+#define SM(arr, z, x) ((arr) + ((x) + NO) * T.MZ + ((z) + OM))
+#define GX(arr, z, L) ((arr) + ((L) + NO) * TZe + (z))
+#define GZ(arr, L, x) ((arr) + (x) * T.ZW + ((L) + OM))
+
     const float rdx = 1.0f / a.dx, rdz = 1.0f / a.dz;
     const float* uxc = a.ux[a.cur];
     const float* uzc = a.uz[a.cur];
 
-    // ---- phase 0: field tile (with injection) and material tile -------------
-    // kFill items per thread per round: every load of a round is issued before the first
-    // shared-memory store, so a round costs one memory latency.
-    constexpr int kFill = 4;
-    Walk wu(tid, T.UZ, kThreads);     // (i % UZ, i / UZ) of this thread's items, in order
-    for (int i0 = tid; i0 < T.U; i0 += kFill * kThreads) {
-        float vx[kFill], vz[kFill], bx[kFill], bz[kFill];
+    // ---- phase 0: field tile and material tile, by row pairs; then the background strips -----
+    // Every load of a round is issued before the first shared-memory store, so a round costs one
+    // memory latency.
+    {
+        constexpr int kFill = 4;
+        const int P2 = T.UZ / 2, NP = P2 * T.UX;
+        Walk wu(tid, P2, kThreads);   // (pair row, column) of this thread's items, in order
+        for (int i0 = tid; i0 < NP; i0 += kFill * kThreads) {
+            float2 vx[kFill], vz[kFill];
 #pragma unroll
-        for (int q = 0; q < kFill; ++q) {
-            const int i = i0 + q * kThreads;
-            const int sz = wu.r, sx = wu.q;
-            wu.next();
-            vx[q] = 0.f; vz[q] = 0.f; bx[q] = 0.f; bz[q] = 0.f;
-            if (i < T.U) {
-                const int iz = R.z0 - H + sz, ix = R.x0 - H + sx;
-                if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
-                    const size_t g = gidx(a, iz, ix);
-                    vx[q] = uxc[g];
-                    vz[q] = uzc[g];
-                    const float* pz = nullptr;
-                    const float* px = pml ? inner_bg_ptr(a, iz, ix, pz) : outer_bg_ptr(a, iz, ix, pz);
-                    if (px) {
-                        bx[q] = __ldg(px);
-                        bz[q] = __ldg(pz);
-                    }
+            for (int q = 0; q < kFill; ++q) {
+                const int i = i0 + q * kThreads;
+                const int iz = R.z0 - OU + 2 * wu.r, ix = R.x0 - H + wu.q;
+                wu.next();
+                vx[q] = f2s(0.f);
+                vz[q] = f2s(0.f);
+                if (i < NP && ix >= 1 - npml && ix <= nx + npml) {
+                    const long long g = (long long)(iz - 1) + (long long)(ix + npml - 1) * a.ldz;
+                    if (iz >= 1 && iz <= NZ) { vx[q].x = uxc[g]; vz[q].x = uzc[g]; }
+                    if (iz + 1 >= 1 && iz + 1 <= NZ) { vx[q].y = uxc[g + 1]; vz[q].y = uzc[g + 1]; }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kFill; ++q) {
+                const int i = i0 + q * kThreads;
+                if (i < NP) {
+                    sts2(sux + 2 * i, vx[q]);
+                    sts2(suz + 2 * i, vz[q]);
                 }
             }
         }
+        constexpr int kFillM = 4;
+        const int M2 = T.MZ / 2, NMP = M2 * T.MX;
+        Walk wm(tid, M2, kThreads);
+        for (int i0 = tid; i0 < NMP; i0 += kFillM * kThreads) {
+            float2 l[kFillM], m[kFillM];
 #pragma unroll
-        for (int q = 0; q < kFill; ++q) {
-            const int i = i0 + q * kThreads;
-            if (i < T.U) {
-                sux[i] = pml ? vx[q] - bx[q] : vx[q] + bx[q];
-                suz[i] = pml ? vz[q] - bz[q] : vz[q] + bz[q];
-            }
-        }
-    }
-    Walk wm(tid, T.MZ, kThreads);
-    for (int i0 = tid; i0 < T.M; i0 += kFill * kThreads) {
-        float l[kFill], m[kFill];
-#pragma unroll
-        for (int q = 0; q < kFill; ++q) {
-            const int i = i0 + q * kThreads;
-            const int mz = wm.r, mx = wm.q;
-            wm.next();
-            l[q] = 0.f; m[q] = 1.f;
-            if (i < T.M) {
-                const int iz = R.z0 - NO + mz, ix = R.x0 - NO + mx;
-                if (iz >= 1 && iz <= NZ && ix >= 1 - npml && ix <= nx + npml) {
-                    const size_t g = gidx(a, iz, ix);
-                    l[q] = __ldg(a.lam + g);
-                    m[q] = __ldg(a.mu + g);
+            for (int q = 0; q < kFillM; ++q) {
+                const int i = i0 + q * kThreads;
+                const int iz = R.z0 - OM + 2 * wm.r, ix = R.x0 - NO + wm.q;
+                wm.next();
+                l[q] = f2s(0.f); m[q] = f2s(1.f);
+                if (i < NMP && ix >= 1 - npml && ix <= nx + npml) {
+                    const long long g = (long long)(iz - 1) + (long long)(ix + npml - 1) * a.ldz;
+                    if (iz >= 1 && iz <= NZ) { l[q].x = __ldg(a.lam + g); m[q].x = __ldg(a.mu + g); }
+                    if (iz + 1 >= 1 && iz + 1 <= NZ) { l[q].y = __ldg(a.lam + g + 1); m[q].y = __ldg(a.mu + g + 1); }
                 }
             }
-        }
 #pragma unroll
-        for (int q = 0; q < kFill; ++q) {
-            const int i = i0 + q * kThreads;
-            if (i < T.M) {
-                const float l2 = l[q] + 2.0f * m[q];
-                sLam[i] = l[q];
-                sMu[i] = m[q];
-                sRL2m[i] = fast_rcp(l2);
-                sRMu[i] = fast_rcp(m[q]);
+            for (int q = 0; q < kFillM; ++q) {
+                const int i = i0 + q * kThreads;
+                if (i < NMP) {
+                    const float2 l2 = pfma(f2s(2.0f), m[q], l[q]);   // lambda + 2 mu (2 mu exact)
+                    sts2(sLam + 2 * i, l[q]);
+                    sts2(sMu + 2 * i, m[q]);
+                    sts2(sRL2m + 2 * i, f2(fast_rcp(l2.x), fast_rcp(l2.y)));
+                    sts2(sRMu + 2 * i, f2(fast_rcp(m[q].x), fast_rcp(m[q].y)));
+                }
             }
         }
     }
     __syncthreads();
-
-#define SU(arr, z, x) arr[((x) + H) * T.UZ + ((z) + H)]
-#define SM(arr, z, x) arr[((x) + NO) * T.MZ + ((z) + NO)]
+    // the background strips that meet the u tile, added (regular field) or removed (absorbing
+    // layers' operator field) in place: one rounding per value, as u + b / u - b
+    {
+        const int zt0 = R.z0 - OU, zt1 = R.z0 - OU + T.UZ - 1;
+        const int xt0 = R.x0 - H, xt1 = R.x0 - H + T.UX - 1;
+#pragma unroll 1
+        for (int k = 0; k < 3; ++k) {
+            const StripRect S = strip_rect(a, pml, k);
+            const int z0 = max(max(S.zr0, 1), zt0), z1 = min(S.zr1, zt1);
+            // the right strips start after the left ones where the two would meet (narrow grids)
+            const int x0 = max(k == 1 && pml ? max(S.xr0, a.nbd + 1) : S.xr0, xt0), x1 = min(S.xr1, xt1);
+            if (z0 > z1 || x0 > x1) continue;
+            const int nzr = z1 - z0 + 1, n = nzr * (x1 - x0 + 1);
+            const long long plane = (long long)S.rows * S.cols * a.it;
+            const float* bxs = a.strip[S.sx] + plane;
+            const float* bzs = a.strip[S.sz] + plane;
+            for (int e = tid; e < n; e += kThreads) {
+                int xq, zr;
+                divmod_small(e, nzr, xq, zr);
+                const int iz = z0 + zr, ix = x0 + xq;
+                const long long o = (long long)(iz - S.zr0) + (long long)S.rows * (ix - S.xr0);
+                float* px = SU(sux, iz - R.z0, ix - R.x0);
+                float* pz = SU(suz, iz - R.z0, ix - R.x0);
+                const float bx = __ldg(bxs + o), bz = __ldg(bzs + o);
+                *px = pml ? __fsub_rn(*px, bx) : __fadd_rn(*px, bx);
+                *pz = pml ? __fsub_rn(*pz, bz) : __fadd_rn(*pz, bz);
+            }
+        }
+    }
+    __syncthreads();
 
     // ---- free surface (row 1, stress image about row 1.5): its terms per column, once -------
     // Formed here by one thread per column rather than inside the output loop, where the row-1
@@ -394,352 +482,410 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             float dA = 0.f, dB = 0.f, dz1 = 0.f, dz2v = 0.f, dx1 = 0.f, dx2v = 0.f;
 #pragma unroll
             for (int k = 1; k <= NO; ++k) {
-                float c = c_coll[nxo][k];
-                float Ap = SM(sLam, 0, x + k) * (SU(suz, 1, x + k) - SU(suz, 0, x + k)) / dz;
-                float Am = SM(sLam, 0, x - k) * (SU(suz, 1, x - k) - SU(suz, 0, x - k)) / dz;
-                float Bp = SM(sMu, 0, x + k) * (SU(sux, 1, x + k) - SU(sux, 0, x + k)) / dz;
-                float Bm = SM(sMu, 0, x - k) * (SU(sux, 1, x - k) - SU(sux, 0, x - k)) / dz;
-                dA = fmaf(c, Ap - Am, dA);
-                dB = fmaf(c, Bp - Bm, dB);
-                dz1 = fmaf(c, SU(suz, 0, x + k) - SU(suz, 0, x - k), dz1);
-                dz2v = fmaf(c, SU(suz, 1, x + k) - SU(suz, 1, x - k), dz2v);
-                dx1 = fmaf(c, SU(sux, 0, x + k) - SU(sux, 0, x - k), dx1);
-                dx2v = fmaf(c, SU(sux, 1, x + k) - SU(sux, 1, x - k), dx2v);
+                const float c = c_coll[nxo][k];
+                const float Ap = __fdiv_rn(__fmul_rn(*SM(sLam, 0, x + k), __fsub_rn(*SU(suz, 1, x + k), *SU(suz, 0, x + k))), dz);
+                const float Am = __fdiv_rn(__fmul_rn(*SM(sLam, 0, x - k), __fsub_rn(*SU(suz, 1, x - k), *SU(suz, 0, x - k))), dz);
+                const float Bp = __fdiv_rn(__fmul_rn(*SM(sMu, 0, x + k), __fsub_rn(*SU(sux, 1, x + k), *SU(sux, 0, x + k))), dz);
+                const float Bm = __fdiv_rn(__fmul_rn(*SM(sMu, 0, x - k), __fsub_rn(*SU(sux, 1, x - k), *SU(sux, 0, x - k))), dz);
+                dA = fmaf(c, __fsub_rn(Ap, Am), dA);
+                dB = fmaf(c, __fsub_rn(Bp, Bm), dB);
+                dz1 = fmaf(c, __fsub_rn(*SU(suz, 0, x + k), *SU(suz, 0, x - k)), dz1);
+                dz2v = fmaf(c, __fsub_rn(*SU(suz, 1, x + k), *SU(suz, 1, x - k)), dz2v);
+                dx1 = fmaf(c, __fsub_rn(*SU(sux, 0, x + k), *SU(sux, 0, x - k)), dx1);
+                dx2v = fmaf(c, __fsub_rn(*SU(sux, 1, x + k), *SU(sux, 1, x - k)), dx2v);
             }
-            dA /= dx; dB /= dx; dz1 /= dx; dz2v /= dx; dx1 /= dx; dx2v /= dx;
-            const float mu1 = SM(sMu, 0, x), mu2 = SM(sMu, 1, x);
-            const float la1 = SM(sLam, 0, x), la2 = SM(sLam, 1, x);
-            const float hmu = 2.0f / (SM(sRMu, 0, x) + SM(sRMu, 1, x));
-            const float hl2m = 2.0f / (SM(sRL2m, 0, x) + SM(sRL2m, 1, x));
-            const float dux = SU(sux, 1, x) - SU(sux, 0, x);
-            const float duz = SU(suz, 1, x) - SU(suz, 0, x);
-            const float fsA = dA;                                   // Dx[lam(1) dz uz]
-            const float fsB = dB;                                   // Dx[mu(1)  dz ux]
-            const float fsx = hmu * dux / dz;                       // z part of sxz(1.5)
-            const float fsz = hl2m * duz / dz;                      // z part of szz(1.5)
-            // x parts of the half-row stresses
-            const float dux1 = 0.5f * (mu1 * dz1 + mu2 * dz2v);     // (mu1 Dx uz1 + mu2 Dx uz2)/2
-            const float duz1 = 0.5f * (la1 * dx1 + la2 * dx2v);     // (lam1 Dx ux1 + lam2 Dx ux2)/2
-            sFS[kFsA * TX + x] = fsA;
-            sFS[kFsQx * TX + x] = 2.0f * (fsx + dux1) / dz;
-            sFS[kFsB * TX + x] = fsB;
-            sFS[kFsQz * TX + x] = 2.0f * (fsz + duz1) / dz;
-            sFS[kFsF2x * TX + x] = fsA + 2.0f * dux1 / dz;
-            sFS[kFsF3x * TX + x] = 2.0f * fsx / dz;
-            sFS[kFsF2z * TX + x] = fsB + 2.0f * duz1 / dz;
-            sFS[kFsF3z * TX + x] = 2.0f * fsz / dz;
+            dA = __fdiv_rn(dA, dx); dB = __fdiv_rn(dB, dx);
+            dz1 = __fdiv_rn(dz1, dx); dz2v = __fdiv_rn(dz2v, dx);
+            dx1 = __fdiv_rn(dx1, dx); dx2v = __fdiv_rn(dx2v, dx);
+            const float mu1 = *SM(sMu, 0, x), mu2 = *SM(sMu, 1, x);
+            const float la1 = *SM(sLam, 0, x), la2 = *SM(sLam, 1, x);
+            const float hmu = __fdiv_rn(2.0f, __fadd_rn(*SM(sRMu, 0, x), *SM(sRMu, 1, x)));
+            const float hl2m = __fdiv_rn(2.0f, __fadd_rn(*SM(sRL2m, 0, x), *SM(sRL2m, 1, x)));
+            const float dux = __fsub_rn(*SU(sux, 1, x), *SU(sux, 0, x));
+            const float duz = __fsub_rn(*SU(suz, 1, x), *SU(suz, 0, x));
+            // Dx[lam(1) dz uz], Dx[mu(1) dz ux]; z parts of sxz(1.5), szz(1.5)
+            const float fsx = __fdiv_rn(__fmul_rn(hmu, dux), dz);
+            const float fsz = __fdiv_rn(__fmul_rn(hl2m, duz), dz);
+            // x parts of the half-row stresses: (mu1 Dx uz1 + mu2 Dx uz2)/2, (lam1 Dx ux1 + lam2 Dx ux2)/2
+            const float dux1 = __fmul_rn(0.5f, fmaf(mu1, dz1, __fmul_rn(mu2, dz2v)));
+            const float duz1 = __fmul_rn(0.5f, fmaf(la1, dx1, __fmul_rn(la2, dx2v)));
+            sFS[kFsA * TX + x] = dA;
+            sFS[kFsQx * TX + x] = __fdiv_rn(__fmul_rn(2.0f, __fadd_rn(fsx, dux1)), dz);
+            sFS[kFsB * TX + x] = dB;
+            sFS[kFsQz * TX + x] = __fdiv_rn(__fmul_rn(2.0f, __fadd_rn(fsz, duz1)), dz);
+            sFS[kFsF2x * TX + x] = __fadd_rn(dA, __fdiv_rn(__fmul_rn(2.0f, dux1), dz));
+            sFS[kFsF3x * TX + x] = __fdiv_rn(__fmul_rn(2.0f, fsx), dz);
+            sFS[kFsF2z * TX + x] = __fadd_rn(dB, __fdiv_rn(__fmul_rn(2.0f, duz1), dz));
+            sFS[kFsF3z * TX + x] = __fdiv_rn(__fmul_rn(2.0f, fsz), dz);
         }
     }
 
-    // ---- phase 1a: x-direction staggered products and dzx operands -----------
-    Walk w1(tid, TZ, kThreads);
-    for (int i = tid; i < T.AX; i += kThreads, w1.next()) {
-        const int z = w1.r, xl = w1.q;
-        int iz = R.z0 + z;
-        // staggered product at label L = xl - NO (half point between L and L+1)
-        if (xl < T.XW - 1) {
-            int L = xl - NO;
-            int n = ordx(a, R.x0 + L, NO);
-            float sx = 0.f, szv = 0.f;
+    // ---- phase 1a: x-direction staggered products and dzx operands, by row pairs -----------
+    {
+        const int PZ = TZe / 2;
+        Walk w1(tid, PZ, kThreads);
+        for (int i = tid; i < PZ * T.XW; i += kThreads, w1.next()) {
+            const int z = 2 * w1.r, xl = w1.q;
+            const int iz = R.z0 + z;
+            const int o = xl * TZe + z;
+            // staggered products at label L = xl - NO (half point between columns L and L+1)
+            if (xl < T.XW - 1) {
+                const int L = xl - NO;
+                const int n = ordx(a, R.x0 + L, NO);
+                float2 sx = f2s(0.f), szv = f2s(0.f);
 #pragma unroll
-            for (int j = 1; j <= NO; ++j) {
-                float c = c_stag[n][j];
-                sx = fmaf(c, SU(sux, z, L + j) - SU(sux, z, L + 1 - j), sx);
-                szv = fmaf(c, SU(suz, z, L + j) - SU(suz, z, L + 1 - j), szv);
+                for (int j = 1; j <= NO; ++j) {
+                    const float2 c = f2s(c_stag[n][j]);
+                    sx = pfma(c, psub(lds2(SU(sux, z, L + j)), lds2(SU(sux, z, L + 1 - j))), sx);
+                    szv = pfma(c, psub(lds2(SU(suz, z, L + j)), lds2(SU(suz, z, L + 1 - j))), szv);
+                }
+                const float2 rl = padd(lds2(SM(sRL2m, z, L)), lds2(SM(sRL2m, z, L + 1)));
+                const float2 rm = padd(lds2(SM(sRMu, z, L)), lds2(SM(sRMu, z, L + 1)));
+                sts2(gxA + o, pmul(f2(2.0f * fast_rcp(rl.x), 2.0f * fast_rcp(rl.y)), sx));
+                sts2(gxB + o, pmul(f2(2.0f * fast_rcp(rm.x), 2.0f * fast_rcp(rm.y)), szv));
             }
-            float hl = 2.0f * fast_rcp(SM(sRL2m, z, L) + SM(sRL2m, z, L + 1));
-            float hm = 2.0f * fast_rcp(SM(sRMu, z, L) + SM(sRMu, z, L + 1));
-            gxA[i] = hl * sx;
-            gxB[i] = hm * szv;
-        }
-        // dzx operands at cell column x = xl - NO
-        {
-            int x = xl - NO;
-            int ix = R.x0 + x;
-            int n = ordz(a, iz, NO);
-            float dzz = 0.f, dzx = 0.f;
+            // dzx operands at column x = xl - NO
+            {
+                const int x = xl - NO;
+                const int ix = R.x0 + x;
+                const int n0 = ordz(a, iz, NO), n1 = ordz(a, iz + 1, NO);
+                float wz[NWIN], wx[NWIN];
+                load_rows(SU(suz, z - OM, x), wz);
+                load_rows(SU(sux, z - OM, x), wx);
+                float2 dzz = f2s(0.f), dzx = f2s(0.f);
 #pragma unroll
-            for (int k = 1; k <= NO; ++k) {
-                float c = c_coll[n][k];
-                dzz = fmaf(c, SU(suz, z + k, x) - SU(suz, z - k, x), dzz);
-                dzx = fmaf(c, SU(sux, z + k, x) - SU(sux, z - k, x), dzx);
+                for (int k = 1; k <= NO; ++k) {
+                    const float2 c = f2(c_coll[n0][k], c_coll[n1][k]);
+                    dzz = pfma(c, f2(__fsub_rn(wz[OM + k], wz[OM - k]), __fsub_rn(wz[OM + 1 + k], wz[OM + 1 - k])), dzz);
+                    dzx = pfma(c, f2(__fsub_rn(wx[OM + k], wx[OM - k]), __fsub_rn(wx[OM + 1 + k], wx[OM + 1 - k])), dzx);
+                }
+                // diffzx_reg forms v on rows 2..nz; diffzx_pml on rows 2..NZ-1, columns 2-npml..nx+npml-1
+                const bool colv = pml ? (ix >= 2 - npml && ix <= nx + npml - 1) : (ix >= 1 - NO && ix <= nx + NO);
+                const int zmax = pml ? NZ - 1 : nz;
+                float2 a1 = pmul(pmul(lds2(SM(sLam, z, x)), dzz), f2s(rdz));
+                float2 a4 = pmul(pmul(lds2(SM(sMu, z, x)), dzx), f2s(rdz));
+                if (!(colv && iz >= 2 && iz <= zmax)) { a1.x = 0.f; a4.x = 0.f; }
+                if (!(colv && iz + 1 >= 2 && iz + 1 <= zmax)) { a1.y = 0.f; a4.y = 0.f; }
+                sts2(v1 + o, a1);
+                sts2(v4 + o, a4);
             }
-            // diffzx_reg forms v on rows 2..nz; diffzx_pml on rows 2..NZ-1, columns 2-npml..nx+npml-1
-            bool valid = pml ? (iz >= 2 && iz <= NZ - 1 && ix >= 2 - npml && ix <= nx + npml - 1)
-                             : (iz >= 2 && iz <= nz && ix >= 1 - NO && ix <= nx + NO);
-            v1[i] = valid ? SM(sLam, z, x) * dzz * rdz : 0.f;
-            v4[i] = valid ? SM(sMu, z, x) * dzx * rdz : 0.f;
         }
     }
-    // ---- phase 1b: z-direction staggered products and dxz operands -----------
-    Walk w2(tid, T.ZW, kThreads);
-    for (int i = tid; i < T.AZ; i += kThreads, w2.next()) {
-        const int zl = w2.r, x = w2.q;
-        int ix = R.x0 + x;
-        if (zl < T.ZW - 1) {
-            int L = zl - NO;
-            int n = ordz(a, R.z0 + L, NO);
-            float sz_ = 0.f, sx = 0.f;
+    // ---- phase 1b: z-direction staggered products and dxz operands, by row pairs -----------
+    {
+        const int PZ = T.ZW / 2;
+        Walk w2(tid, PZ, kThreads);
+        for (int i = tid; i < PZ * TX; i += kThreads, w2.next()) {
+            const int L = 2 * w2.r - OM, x = w2.q;   // rows / half-point labels L, L+1
+            const int ix = R.x0 + x;
+            const int o = x * T.ZW + (L + OM);
+            if (L <= TZ + NO - 2) {   // labels read by the output cells: -NO .. TZ+NO-2
+                const int n0 = ordz(a, R.z0 + L, NO), n1 = ordz(a, R.z0 + L + 1, NO);
+                // rows L+1-NO .. L+1+NO from the even row L - B
+                constexpr int B = 2 * (NO / 2);
+                float wz[NO + B + 2], wx[NO + B + 2];
+                load_rows(SU(suz, L - B, x), wz);
+                load_rows(SU(sux, L - B, x), wx);
+                float2 szv = f2s(0.f), sx = f2s(0.f);
 #pragma unroll
-            for (int j = 1; j <= NO; ++j) {
-                float c = c_stag[n][j];
-                sz_ = fmaf(c, SU(suz, L + j, x) - SU(suz, L + 1 - j, x), sz_);
-                sx = fmaf(c, SU(sux, L + j, x) - SU(sux, L + 1 - j, x), sx);
+                for (int j = 1; j <= NO; ++j) {
+                    const float2 c = f2(c_stag[n0][j], c_stag[n1][j]);
+                    // half point L: u(L+j) - u(L+1-j); half point L+1: u(L+1+j) - u(L+2-j)
+                    szv = pfma(c, f2(__fsub_rn(wz[B + j], wz[B + 1 - j]), __fsub_rn(wz[B + 1 + j], wz[B + 2 - j])), szv);
+                    sx = pfma(c, f2(__fsub_rn(wx[B + j], wx[B + 1 - j]), __fsub_rn(wx[B + 1 + j], wx[B + 2 - j])), sx);
+                }
+                // harmonic means over rows (L, L+1) and (L+1, L+2); row L+2 only where half point
+                // L+1 is read (the material tile ends at row TZe+OM-1)
+                const int L2 = L + 1 <= TZ + NO - 2 ? L + 2 : L + 1;
+                const float2 rl = lds2(SM(sRL2m, L, x)), rm = lds2(SM(sRMu, L, x));
+                const float rl2 = *SM(sRL2m, L2, x), rm2 = *SM(sRMu, L2, x);
+                const float2 hl = f2(2.0f * fast_rcp(__fadd_rn(rl.x, rl.y)), 2.0f * fast_rcp(__fadd_rn(rl.y, rl2)));
+                const float2 hm = f2(2.0f * fast_rcp(__fadd_rn(rm.x, rm.y)), 2.0f * fast_rcp(__fadd_rn(rm.y, rm2)));
+                sts2(gzA + o, pmul(hl, szv));
+                sts2(gzB + o, pmul(hm, sx));
             }
-            float hl = 2.0f * fast_rcp(SM(sRL2m, L, x) + SM(sRL2m, L + 1, x));
-            float hm = 2.0f * fast_rcp(SM(sRMu, L, x) + SM(sRMu, L + 1, x));
-            gzA[i] = hl * sz_;
-            gzB[i] = hm * sx;
-        }
-        {
-            int z = zl - NO;
-            int iz = R.z0 + z;
-            int n = ordx(a, ix, NO);
-            float dxz = 0.f, dxx = 0.f;
+            // dxz operands at rows L, L+1
+            {
+                const int iz = R.z0 + L;
+                const int n = ordx(a, ix, NO);
+                float2 dxz = f2s(0.f), dxx = f2s(0.f);
 #pragma unroll
-            for (int k = 1; k <= NO; ++k) {
-                float c = c_coll[n][k];
-                dxz = fmaf(c, SU(suz, z, x + k) - SU(suz, z, x - k), dxz);
-                dxx = fmaf(c, SU(sux, z, x + k) - SU(sux, z, x - k), dxx);
+                for (int k = 1; k <= NO; ++k) {
+                    const float2 c = f2s(c_coll[n][k]);
+                    dxz = pfma(c, psub(lds2(SU(suz, L, x + k)), lds2(SU(suz, L, x - k))), dxz);
+                    dxx = pfma(c, psub(lds2(SU(sux, L, x + k)), lds2(SU(sux, L, x - k))), dxx);
+                }
+                // diffxz_reg forms v on rows 1..nz+norder, columns 1..nx; diffxz_pml on rows 1..NZ-1
+                const bool colv = pml ? (ix >= 2 - npml && ix <= nx + npml - 1) : (ix >= 1 && ix <= nx);
+                const int zmax = pml ? NZ - 1 : nz + NO;
+                float2 a2 = pmul(pmul(lds2(SM(sMu, L, x)), dxz), f2s(rdx));
+                float2 a3 = pmul(pmul(lds2(SM(sLam, L, x)), dxx), f2s(rdx));
+                if (!(colv && iz >= 1 && iz <= zmax)) { a2.x = 0.f; a3.x = 0.f; }
+                if (!(colv && iz + 1 >= 1 && iz + 1 <= zmax)) { a2.y = 0.f; a3.y = 0.f; }
+                sts2(v2 + o, a2);
+                sts2(v3 + o, a3);
             }
-            // diffxz_reg forms v on rows 1..nz+norder, columns 1..nx; diffxz_pml on rows 1..NZ-1
-            bool valid = pml ? (iz >= 1 && iz <= NZ - 1 && ix >= 2 - npml && ix <= nx + npml - 1)
-                             : (iz >= 1 && iz <= nz + NO && ix >= 1 && ix <= nx);
-            v2[i] = valid ? SM(sMu, z, x) * dxz * rdx : 0.f;
-            v3[i] = valid ? SM(sLam, z, x) * dxx * rdx : 0.f;
         }
     }
     __syncthreads();
 
-#define GXI(arr, z, L) arr[((L) + NO) * TZ + (z)]
-#define VXI(arr, z, x) arr[((x) + NO) * TZ + (z)]
-#define GZI(arr, L, x) arr[(x) * T.ZW + ((L) + NO)]
-#define VZI(arr, z, x) arr[(x) * T.ZW + ((z) + NO)]
-
-    // ---- phase 2: output cells ----------------------------------------------
-    const float dx2 = pml ? a.dx2p : a.dx2r;
-    Walk wc(tid, TZ, kThreads);
-    for (int cell = tid; cell < TZ * TX; cell += kThreads, wc.next()) {
-        const int z = wc.r, x = wc.q;
+    // ---- phase 2: output cells, by row pairs -------------------------------------------
+    const float2 dx2 = f2s(pml ? a.dx2p : a.dx2r), dz2 = f2s(a.dz2);
+    const float2 rdx2 = f2s(rdx), rdz2 = f2s(rdz);
+    float* const uxn = a.ux[a.cur ^ 1];
+    float* const uzn = a.uz[a.cur ^ 1];
+    const int PZ2 = TZe / 2;
+    Walk wc(tid, PZ2, kThreads);
+    for (int cell = tid; cell < PZ2 * TX; cell += kThreads, wc.next()) {
+        const int z = 2 * wc.r, x = wc.q;
         const int iz = R.z0 + z;
         const int ix = R.x0 + x;
-        if (iz < R.zlo || iz > R.zhi || ix < R.xlo || ix > R.xhi) continue;
-        const size_t g = gidx(a, iz, ix);
-        const int nxo = ordx(a, ix, NO);
-        const int nzo = ordz(a, iz, NO);
-        // every column ix-NO..ix (row iz-NO..iz) has the full order: no reduced-order half points
-        const bool fullx = ix - NO >= NO - npml + 1 && ix <= nx + npml - NO;
-        const bool fullz = iz - NO >= NO + 1 && iz <= NZ - NO;
+        // the first row of a pair lies in the tile whenever the second does (z + 1 < TZ implies
+        // z < TZ, rows rise with z), so a pair is skipped or has its first row; its second row
+        // may lie past the tile, the layer or the grid (then it is computed from clamped loads and
+        // never stored)
+        if (ix < R.xlo || ix > R.xhi || iz > R.zhi) continue;
+        const bool in1 = z + 1 < TZ && iz + 1 <= R.zhi;
+        const long long g = (long long)(iz - 1) + (long long)(ix + npml - 1) * a.ldz;
+        const long long g1 = in1 ? g + 1 : g;
 
         if (pml && (ix == 1 - npml || ix == nx + npml || iz == NZ)) {
-            // outer frame: never advanced; keep level 1 across the plane swap
-            a.ux[a.cur ^ 1][g] = uxc[g];
-            a.uz[a.cur ^ 1][g] = uzc[g];
+            // outer frame: never advanced; keep level 1 across the plane swap (a pair that starts
+            // on row NZ has no second row in the layer)
+            uxn[g] = uxc[g];
+            uzn[g] = uzc[g];
+            if (in1) { uxn[g1] = uxc[g1]; uzn[g1] = uzc[g1]; }
             continue;
         }
 
-        const float kd = __ldg(a.kdt2 + g);
+        const int nxo = ordx(a, ix, NO);
+        const int nz0 = ordz(a, iz, NO), nz1 = ordz(a, iz + 1, NO);
+        // every column ix-NO..ix (row iz-NO..iz) has the full order: no reduced-order half points
+        const bool fullx = ix - NO >= NO - npml + 1 && ix <= nx + npml - NO;
+        const bool fullz0 = iz - NO >= NO + 1 && iz <= NZ - NO;
+        const bool fullz1 = iz + 1 - NO >= NO + 1 && iz + 1 <= NZ - NO;
+        const float2 kd = f2(__ldg(a.kdt2 + g), __ldg(a.kdt2 + g1));
 
         // x-direction second derivatives dxx(l2m ux), dxx(mu uz)
-        float x2a = 0.f, x2b = 0.f;
+        float2 x2a = f2s(0.f), x2b = f2s(0.f);
 #pragma unroll
         for (int k = 1; k <= NO; ++k) {
-            float c = c_stag[nxo][k];
-            float pa = GXI(gxA, z, x + k - 1), pb = GXI(gxB, z, x + k - 1);
-            float ma, mb;
-            int Lm = x - k;
-            int nr = fullx ? NO : ordx(a, ix - k + 1, NO);
+            const float2 c = f2s(c_stag[nxo][k]);
+            const float2 pa = lds2(GX(gxA, z, x + k - 1)), pb = lds2(GX(gxB, z, x + k - 1));
+            float2 ma, mb;
+            const int Lm = x - k;
+            const int nr = fullx ? NO : ordx(a, ix - k + 1, NO);
             if (fullx || nr == ordx(a, ix - k, NO)) {
-                ma = GXI(gxA, z, Lm); mb = GXI(gxB, z, Lm);
+                ma = lds2(GX(gxA, z, Lm));
+                mb = lds2(GX(gxB, z, Lm));
             } else {
-                float s1 = 0.f, s2 = 0.f;
+                float2 s1 = f2s(0.f), s2 = f2s(0.f);
                 for (int j = 1; j <= NO; ++j) {
-                    float cj = c_stag[nr][j];
-                    s1 = fmaf(cj, SU(sux, z, Lm + j) - SU(sux, z, Lm + 1 - j), s1);
-                    s2 = fmaf(cj, SU(suz, z, Lm + j) - SU(suz, z, Lm + 1 - j), s2);
+                    const float2 cj = f2s(c_stag[nr][j]);
+                    s1 = pfma(cj, psub(lds2(SU(sux, z, Lm + j)), lds2(SU(sux, z, Lm + 1 - j))), s1);
+                    s2 = pfma(cj, psub(lds2(SU(suz, z, Lm + j)), lds2(SU(suz, z, Lm + 1 - j))), s2);
                 }
-                ma = 2.0f / (SM(sRL2m, z, Lm) + SM(sRL2m, z, Lm + 1)) * s1;
-                mb = 2.0f / (SM(sRMu, z, Lm) + SM(sRMu, z, Lm + 1)) * s2;
+                const float2 rl = padd(lds2(SM(sRL2m, z, Lm)), lds2(SM(sRL2m, z, Lm + 1)));
+                const float2 rm = padd(lds2(SM(sRMu, z, Lm)), lds2(SM(sRMu, z, Lm + 1)));
+                ma = pmul(f2(__fdiv_rn(2.0f, rl.x), __fdiv_rn(2.0f, rl.y)), s1);
+                mb = pmul(f2(__fdiv_rn(2.0f, rm.x), __fdiv_rn(2.0f, rm.y)), s2);
             }
-            x2a = fmaf(c, pa - ma, x2a);
-            x2b = fmaf(c, pb - mb, x2b);
+            x2a = pfma(c, psub(pa, ma), x2a);
+            x2b = pfma(c, psub(pb, mb), x2b);
         }
-        const float Fx2_l2m_ux = x2a * dx2;
-        const float Fx2_mu_uz = x2b * dx2;
+        const float2 Fx2_l2m_ux = pmul(x2a, dx2);
+        const float2 Fx2_mu_uz = pmul(x2b, dx2);
 
-        // z-direction second derivatives dzz(l2m uz), dzz(mu ux)
-        float z2a = 0.f, z2b = 0.f;
+        // z-direction second derivatives dzz(l2m uz), dzz(mu ux); the products at the reduced-order
+        // half points next to the top rows and the outer frame are recomputed with the cell's order
+        float2 z2a = f2s(0.f), z2b = f2s(0.f);
+        {
+            float ga[OM + NO + 1], gb[OM + NO + 1];   // labels z-OM .. z+NO
+            load_rows(GZ(gzA, z - OM, x), ga);
+            load_rows(GZ(gzB, z - OM, x), gb);
 #pragma unroll
-        for (int k = 1; k <= NO; ++k) {
-            float c = c_stag[nzo][k];
-            float pa = GZI(gzA, z + k - 1, x), pb = GZI(gzB, z + k - 1, x);
-            float ma, mb;
-            int Lm = z - k;
-            int nr = fullz ? NO : ordz(a, iz - k + 1, NO);
-            if (fullz || nr == ordz(a, iz - k, NO)) {
-                ma = GZI(gzA, Lm, x); mb = GZI(gzB, Lm, x);
-            } else {
-                float s1 = 0.f, s2 = 0.f;
-                for (int j = 1; j <= NO; ++j) {
-                    float cj = c_stag[nr][j];
-                    s1 = fmaf(cj, SU(suz, Lm + j, x) - SU(suz, Lm + 1 - j, x), s1);
-                    s2 = fmaf(cj, SU(sux, Lm + j, x) - SU(sux, Lm + 1 - j, x), s2);
+            for (int k = 1; k <= NO; ++k) {
+                const float2 c = f2(c_stag[nz0][k], c_stag[nz1][k]);
+                float ma0 = ga[OM - k], ma1 = ga[OM + 1 - k], mb0 = gb[OM - k], mb1 = gb[OM + 1 - k];
+                if (!(fullz0 && fullz1)) {
+#pragma unroll
+                    for (int r = 0; r < 2; ++r) {
+                        const int izr = iz + r;
+                        const int nr = ordz(a, izr - k + 1, NO);
+                        if ((r == 0 ? fullz0 : fullz1) || nr == ordz(a, izr - k, NO)) continue;
+                        const int Lm = z + r - k;
+                        float s1 = 0.f, s2 = 0.f;
+                        for (int j = 1; j <= NO; ++j) {
+                            const float cj = c_stag[nr][j];
+                            s1 = fmaf(cj, __fsub_rn(*SU(suz, Lm + j, x), *SU(suz, Lm + 1 - j, x)), s1);
+                            s2 = fmaf(cj, __fsub_rn(*SU(sux, Lm + j, x), *SU(sux, Lm + 1 - j, x)), s2);
+                        }
+                        const float ra = __fmul_rn(__fdiv_rn(2.0f, __fadd_rn(*SM(sRL2m, Lm, x), *SM(sRL2m, Lm + 1, x))), s1);
+                        const float rb = __fmul_rn(__fdiv_rn(2.0f, __fadd_rn(*SM(sRMu, Lm, x), *SM(sRMu, Lm + 1, x))), s2);
+                        if (r == 0) { ma0 = ra; mb0 = rb; }
+                        else { ma1 = ra; mb1 = rb; }
+                    }
                 }
-                ma = 2.0f / (SM(sRL2m, Lm, x) + SM(sRL2m, Lm + 1, x)) * s1;
-                mb = 2.0f / (SM(sRMu, Lm, x) + SM(sRMu, Lm + 1, x)) * s2;
+                z2a = pfma(c, f2(__fsub_rn(ga[OM + k - 1], ma0), __fsub_rn(ga[OM + k], ma1)), z2a);
+                z2b = pfma(c, f2(__fsub_rn(gb[OM + k - 1], mb0), __fsub_rn(gb[OM + k], mb1)), z2b);
             }
-            z2a = fmaf(c, pa - ma, z2a);
-            z2b = fmaf(c, pb - mb, z2b);
         }
-        const float Fz2_l2m_uz = z2a * a.dz2;
-        const float Fz2_mu_ux = z2b * a.dz2;
+        const float2 Fz2_l2m_uz = pmul(z2a, dz2);
+        const float2 Fz2_mu_ux = pmul(z2b, dz2);
 
         // mixed derivatives
-        float zxl = 0.f, zxm = 0.f, xzm = 0.f, xzl = 0.f;
+        float2 zxl = f2s(0.f), zxm = f2s(0.f), xzm = f2s(0.f), xzl = f2s(0.f);
+        {
+            float w2[NWIN], w3[NWIN];   // rows z-OM .. z+1+NO of v2, v3
+            load_rows(GZ(v2, z - OM, x), w2);
+            load_rows(GZ(v3, z - OM, x), w3);
 #pragma unroll
-        for (int k = 1; k <= NO; ++k) {
-            float cx = c_coll[nxo][k], cz = c_coll[nzo][k];
-            zxl = fmaf(cx, VXI(v1, z, x + k) - VXI(v1, z, x - k), zxl);
-            zxm = fmaf(cx, VXI(v4, z, x + k) - VXI(v4, z, x - k), zxm);
-            xzm = fmaf(cz, VZI(v2, z + k, x) - VZI(v2, z - k, x), xzm);
-            xzl = fmaf(cz, VZI(v3, z + k, x) - VZI(v3, z - k, x), xzl);
+            for (int k = 1; k <= NO; ++k) {
+                const float2 cx = f2s(c_coll[nxo][k]), cz = f2(c_coll[nz0][k], c_coll[nz1][k]);
+                zxl = pfma(cx, psub(lds2(GX(v1, z, x + k)), lds2(GX(v1, z, x - k))), zxl);
+                zxm = pfma(cx, psub(lds2(GX(v4, z, x + k)), lds2(GX(v4, z, x - k))), zxm);
+                xzm = pfma(cz, f2(__fsub_rn(w2[OM + k], w2[OM - k]), __fsub_rn(w2[OM + 1 + k], w2[OM + 1 - k])), xzm);
+                xzl = pfma(cz, f2(__fsub_rn(w3[OM + k], w3[OM - k]), __fsub_rn(w3[OM + 1 + k], w3[OM + 1 - k])), xzl);
+            }
         }
-        const float Fzx_lam_uz = zxl * rdx, Fzx_mu_ux = zxm * rdx;
-        const float Fxz_mu_uz = xzm * rdz, Fxz_lam_ux = xzl * rdz;
-
-        float* uxn = a.ux[a.cur ^ 1];
-        float* uzn = a.uz[a.cur ^ 1];
-        const float ux0 = uxc[g], uz0 = uzc[g];
+        const float2 Fzx_lam_uz = pmul(zxl, rdx2), Fzx_mu_ux = pmul(zxm, rdx2);
+        const float2 Fxz_mu_uz = pmul(xzm, rdz2), Fxz_lam_ux = pmul(xzl, rdz2);
 
         if (!pml) {
-            float Fx, Fz;
-            if (iz == 1) {
-                Fx = Fx2_l2m_ux + sFS[kFsA * TX + x] + sFS[kFsQx * TX + x];
-                Fz = Fx2_mu_uz + sFS[kFsB * TX + x] + sFS[kFsQz * TX + x];
-            } else {
-                Fx = Fx2_l2m_ux + Fzx_lam_uz + Fz2_mu_ux + Fxz_mu_uz;
-                Fz = Fz2_l2m_uz + Fxz_lam_ux + Fx2_mu_uz + Fzx_mu_ux;
+            float2 Fx = padd(padd(padd(Fx2_l2m_ux, Fzx_lam_uz), Fz2_mu_ux), Fxz_mu_uz);
+            float2 Fz = padd(padd(padd(Fz2_l2m_uz, Fxz_lam_ux), Fx2_mu_uz), Fzx_mu_ux);
+            if (iz == 1) {   // the first row of the pair is the free-surface row
+                Fx.x = __fadd_rn(__fadd_rn(Fx2_l2m_ux.x, sFS[kFsA * TX + x]), sFS[kFsQx * TX + x]);
+                Fz.x = __fadd_rn(__fadd_rn(Fx2_mu_uz.x, sFS[kFsB * TX + x]), sFS[kFsQz * TX + x]);
             }
-            uxn[g] = fmaf(kd, Fx, 2.0f * ux0 - uxn[g]);
-            uzn[g] = fmaf(kd, Fz, 2.0f * uz0 - uzn[g]);
+            const float2 ux0 = f2(uxc[g], uxc[g1]), uz0 = f2(uzc[g], uzc[g1]);
+            const float2 uxm = f2(uxn[g], uxn[g1]), uzm = f2(uzn[g], uzn[g1]);
+            const float2 nxv = pfma(kd, Fx, psub(pmul(f2s(2.0f), ux0), uxm));
+            const float2 nzv = pfma(kd, Fz, psub(pmul(f2s(2.0f), uz0), uzm));
+            uxn[g] = nxv.x;
+            uzn[g] = nzv.x;
+            if (in1) { uxn[g1] = nxv.y; uzn[g1] = nzv.y; }
             continue;
         }
 
-        // ---- PML cell: split-field update ----------------------------------
-        // Absorbing-layer state of the cell, gathered in one round of loads (in flight while the
-        // first derivatives below are formed) before any of it is written back.
+        // ---- absorbing-layer cells: split-field update ----------------------------------
         const int side = R.side;
-        size_t ap = 0;
-        float gPx[2], gPz[2], gU1[2], gU1m[2], gU2[2], gU2m[2], gU3[2], gU3m[2];
-        DampCol dxc{0.f, 0.f, 1.f, 1.f}, dzc{0.f, 0.f, 1.f, 1.f};
-        {
-            if (side == 1) ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - (1 - npml));
-            else if (side == 2) ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - nx - 1);
-            else ap = (size_t)(iz - nz - 1) + (size_t)npml * (size_t)(ix - (1 - npml));
-            const int base = side == 1 ? 0 : side == 2 ? 6 : 12;
-            const int bpx0 = side == 1 ? 0 : side == 2 ? 2 : 8;
-#pragma unroll
-            for (int comp = 0; comp < 2; ++comp) {
-                gPx[comp] = a.bp[side == 3 ? bpx0 + 2 * comp : bpx0 + comp][ap];
-                gPz[comp] = side == 3 ? a.bp[9 + 2 * comp][ap] : 0.f;
-                gU1[comp] = a.bu[base + 3 * comp + 0][a.cur][ap];
-                gU1m[comp] = a.bu[base + 3 * comp + 0][a.cur ^ 1][ap];
-                gU2[comp] = a.bu[base + 3 * comp + 1][a.cur][ap];
-                gU2m[comp] = a.bu[base + 3 * comp + 1][a.cur ^ 1][ap];
-                gU3[comp] = a.bu[base + 3 * comp + 2][a.cur][ap];
-                gU3m[comp] = a.bu[base + 3 * comp + 2][a.cur ^ 1][ap];
-            }
-            dxc = a.dampx[ix + npml - 1];
-            if (side == 3) dzc = a.dampz[iz - 1];
-        }
-        const float yx = dxc.y, yz = dzc.y;
-        const float r2 = side == 3 ? fast_rcp(1.0f + 0.5f * (yx + yz)) : dxc.rh;   // 1 / (1 + (yx + yz)/2)
-
-        // first derivatives for the memory variables (diff1 / diffx1 on the PML field)
-        float dxux = 0.f, dxuz = 0.f, dzux = 0.f, dzuz = 0.f;
-#pragma unroll
-        for (int k = 1; k <= NO; ++k) {
-            float cx = c_coll[nxo][k], cz = c_coll[nzo][k];
-            dxux = fmaf(cx, SU(sux, z, x + k) - SU(sux, z, x - k), dxux);
-            dxuz = fmaf(cx, SU(suz, z, x + k) - SU(suz, z, x - k), dxuz);
-            dzux = fmaf(cz, SU(sux, z + k, x) - SU(sux, z - k, x), dzux);
-            dzuz = fmaf(cz, SU(suz, z + k, x) - SU(suz, z - k, x), dzuz);
-        }
-        dxux *= rdx; dxuz *= rdx; dzux *= rdz; dzuz *= rdz;
-        const float lam0 = SM(sLam, z, x), mu0 = SM(sMu, z, x), l2m0 = lam0 + 2.0f * mu0;
-
+        const bool up1 = in1 && iz + 1 != NZ;   // row NZ is outer frame
+        long long ap;   // state index of row iz (row iz+1: ap + 1)
+        if (side == 1) ap = (long long)(iz - 1) + (long long)nz * (ix - (1 - npml));
+        else if (side == 2) ap = (long long)(iz - 1) + (long long)nz * (ix - nx - 1);
+        else ap = (long long)(iz - nz - 1) + (long long)npml * (ix - (1 - npml));
         const int base = side == 1 ? 0 : side == 2 ? 6 : 12;
         const int bpx0 = side == 1 ? 0 : side == 2 ? 2 : 8;
         const int nplane = a.cur ^ 1;
+        const long long ap1 = up1 ? ap + 1 : ap;
+        auto ld = [&](const float* p) { return f2(p[ap], p[ap1]); };
+        auto st = [&](float* p, float2 v) {
+            p[ap] = v.x;
+            if (up1) p[ap1] = v.y;
+        };
+
+        // first derivatives for the memory variables (diff1 / diffx1 on the PML field)
+        float2 dxux = f2s(0.f), dxuz = f2s(0.f), dzux = f2s(0.f), dzuz = f2s(0.f);
+        {
+            float wx[NWIN], wz[NWIN];   // rows z-OM .. z+1+NO
+            load_rows(SU(sux, z - OM, x), wx);
+            load_rows(SU(suz, z - OM, x), wz);
+#pragma unroll
+            for (int k = 1; k <= NO; ++k) {
+                const float2 cx = f2s(c_coll[nxo][k]), cz = f2(c_coll[nz0][k], c_coll[nz1][k]);
+                dxux = pfma(cx, psub(lds2(SU(sux, z, x + k)), lds2(SU(sux, z, x - k))), dxux);
+                dxuz = pfma(cx, psub(lds2(SU(suz, z, x + k)), lds2(SU(suz, z, x - k))), dxuz);
+                dzux = pfma(cz, f2(__fsub_rn(wx[OM + k], wx[OM - k]), __fsub_rn(wx[OM + 1 + k], wx[OM + 1 - k])), dzux);
+                dzuz = pfma(cz, f2(__fsub_rn(wz[OM + k], wz[OM - k]), __fsub_rn(wz[OM + 1 + k], wz[OM + 1 - k])), dzuz);
+            }
+        }
+        dxux = pmul(dxux, rdx2); dxuz = pmul(dxuz, rdx2);
+        dzux = pmul(dzux, rdz2); dzuz = pmul(dzuz, rdz2);
+        const float2 lam0 = lds2(SM(sLam, z, x)), mu0 = lds2(SM(sMu, z, x));
+        const float2 l2m0 = pfma(f2s(2.0f), mu0, lam0);
+
+        const DampCol dxc = a.dampx[ix + npml - 1];
+        DampCol dzc0{0.f, 0.f, 1.f, 1.f}, dzc1{0.f, 0.f, 1.f, 1.f};
+        if (side == 3) {
+            dzc0 = a.dampz[iz - 1];
+            dzc1 = a.dampz[iz + 1 <= NZ ? iz : iz - 1];
+        }
+        const float2 yx = f2s(dxc.y), yz = f2(dzc0.y, dzc1.y);
+        // split 2: (2 - yx yz) u - (1 - (yx + yz)/2) u^{n-1}, over 1 + (yx + yz)/2
+        const float2 hs = pmul(f2s(0.5f), padd(yx, yz));
+        const float2 A2 = pfma(f2s(-dxc.y), yz, f2s(2.0f));
+        const float2 B2 = psub(f2s(1.0f), hs);
+        const float2 r2 = side == 3 ? f2(fast_rcp(__fadd_rn(1.0f, hs.x)), fast_rcp(__fadd_rn(1.0f, hs.y))) : f2s(dxc.rh);
+        // split 1 (x damping): (2 - yx^2) u - (1 - yx) u^{n-1}
+        const float2 A1 = f2s(fmaf(-dxc.y, dxc.y, 2.0f)), B1 = f2s(__fsub_rn(1.0f, dxc.y));
+        const float2 Cx = f2s(__fsub_rn(1.0f, __fmul_rn(0.5f, dxc.y)));   // 1 - yx/2
 #pragma unroll
         for (int comp = 0; comp < 2; ++comp) {
-            float F1, F2, F3, S1, S3 = 0.f;
-            if (iz == 1) {
-                if (comp == 0) {
-                    F1 = Fx2_l2m_ux;
-                    F2 = sFS[kFsF2x * TX + x];
-                    F3 = sFS[kFsF3x * TX + x];
-                    S1 = l2m0 * dxux;
-                } else {
-                    F1 = Fx2_mu_uz;
-                    F2 = sFS[kFsF2z * TX + x];
-                    F3 = sFS[kFsF3z * TX + x];
-                    S1 = mu0 * dxuz;
-                }
-            } else if (comp == 0) {
+            float2 F1, F2, F3, S1, S3;
+            if (comp == 0) {
                 F1 = Fx2_l2m_ux;
-                F2 = Fzx_lam_uz + Fxz_mu_uz;
+                F2 = padd(Fzx_lam_uz, Fxz_mu_uz);
                 F3 = Fz2_mu_ux;
-                S1 = l2m0 * dxux;
-                S3 = mu0 * dzux;
+                S1 = pmul(l2m0, dxux);
+                S3 = pmul(mu0, dzux);
             } else {
                 F1 = Fx2_mu_uz;
-                F2 = Fxz_lam_ux + Fzx_mu_ux;
+                F2 = padd(Fxz_lam_ux, Fzx_mu_ux);
                 F3 = Fz2_l2m_uz;
-                S1 = mu0 * dxuz;
-                S3 = l2m0 * dzuz;
+                S1 = pmul(mu0, dxuz);
+                S3 = pmul(l2m0, dzuz);
             }
-            (void)lam0;
+            if (iz == 1) {   // free-surface row of a side layer (first row of the pair)
+                F2.x = sFS[(comp == 0 ? kFsF2x : kFsF2z) * TX + x];
+                F3.x = sFS[(comp == 0 ? kFsF3x : kFsF3z) * TX + x];
+            }
             float* bpx = a.bp[side == 3 ? bpx0 + 2 * comp : bpx0 + comp];
-            const float Px = gPx[comp];
-            const float Pxn = ((1.0f - 0.5f * yx) * Px - dxc.dtdp * S1) * dxc.rh;
-            bpx[ap] = Pxn;
-            float* b1n = a.bu[base + 3 * comp + 0][nplane];
-            float* b2n = a.bu[base + 3 * comp + 1][nplane];
-            float* b3n = a.bu[base + 3 * comp + 2][nplane];
-            const float u1 = gU1[comp], u1m = gU1m[comp];
-            const float f1 = kd * (F1 + 0.5f * (Pxn + Px));
-            float n1;
-            if (side == 2 && iz != 1)
-                n1 = ((2.0f - yx * yx) * u1 - (1.0f - yx) * u1m) * dxc.r1 + f1;
-            else
-                n1 = ((2.0f - yx * yx) * u1 - (1.0f - yx) * u1m + f1) * dxc.r1;
-            const float u2 = gU2[comp], u2m = gU2m[comp];
-            const float n2 = ((2.0f - yx * yz) * u2 - (1.0f - 0.5f * (yx + yz)) * u2m + kd * F2) * r2;
-            const float u3 = gU3[comp], u3m = gU3m[comp];
-            float n3;
+            const float2 Px = ld(bpx);
+            // memory variable: ((1 - yx/2) Px - dt d' S1) / (1 + yx/2)
+            const float2 Pxn = pmul(pfma(f2s(-dxc.dtdp), S1, pmul(Cx, Px)), f2s(dxc.rh));
+            const float2 u1 = ld(a.bu[base + 3 * comp + 0][a.cur]), u1m = ld(a.bu[base + 3 * comp + 0][nplane]);
+            const float2 u2 = ld(a.bu[base + 3 * comp + 1][a.cur]), u2m = ld(a.bu[base + 3 * comp + 1][nplane]);
+            const float2 u3 = ld(a.bu[base + 3 * comp + 2][a.cur]), u3m = ld(a.bu[base + 3 * comp + 2][nplane]);
+            const float2 f1 = pmul(kd, pfma(f2s(0.5f), padd(Pxn, Px), F1));   // kd (F1 + (Pxn + Px)/2)
+            const float2 t1 = pfma(A1, u1, pmul(f2s(-B1.x), u1m));
+            const float2 n1o = pmul(padd(t1, f1), f2s(dxc.r1));
+            float2 n1 = n1o;
+            if (side == 2) {   // right layer below row 1: the force is not divided by 1 + yx
+                const float2 n1r = pfma(t1, f2s(dxc.r1), f1);
+                n1 = f2(iz == 1 ? n1o.x : n1r.x, n1r.y);
+            }
+            const float2 n2 = pmul(pfma(kd, F2, pfma(A2, u2, pmul(f2(-B2.x, -B2.y), u2m))), r2);
+            float2 n3;
             if (side == 3) {
                 float* bpz = a.bp[9 + 2 * comp];
-                const float Pz = gPz[comp];
-                const float Pzn = ((1.0f - 0.5f * yz) * Pz - dzc.dtdp * S3) * dzc.rh;
-                bpz[ap] = Pzn;
-                n3 = ((2.0f - yz * yz) * u3 - (1.0f - yz) * u3m + kd * (F3 + 0.5f * (Pzn + Pz))) * dzc.r1;
+                const float2 Pz = ld(bpz);
+                const float2 Cz = f2(__fsub_rn(1.0f, __fmul_rn(0.5f, dzc0.y)), __fsub_rn(1.0f, __fmul_rn(0.5f, dzc1.y)));
+                const float2 Pzn = pmul(pfma(f2(-dzc0.dtdp, -dzc1.dtdp), S3, pmul(Cz, Pz)), f2(dzc0.rh, dzc1.rh));
+                st(bpz, Pzn);
+                const float2 A3 = pfma(f2(-dzc0.y, -dzc1.y), yz, f2s(2.0f));
+                const float2 B3 = f2(-__fsub_rn(1.0f, dzc0.y), -__fsub_rn(1.0f, dzc1.y));
+                const float2 t3 = pfma(A3, u3, pmul(B3, u3m));
+                n3 = pmul(pfma(kd, pfma(f2s(0.5f), padd(Pzn, Pz), F3), t3), f2(dzc0.r1, dzc1.r1));
             } else {
-                n3 = fmaf(kd, F3, 2.0f * u3 - u3m);
+                n3 = pfma(kd, F3, psub(pmul(f2s(2.0f), u3), u3m));
             }
-            b1n[ap] = n1;
-            b2n[ap] = n2;
-            b3n[ap] = n3;
-            if (comp == 0) uxn[g] = n1 + n2 + n3;
-            else uzn[g] = n1 + n2 + n3;
+            st(bpx, Pxn);
+            st(a.bu[base + 3 * comp + 0][nplane], n1);
+            st(a.bu[base + 3 * comp + 1][nplane], n2);
+            st(a.bu[base + 3 * comp + 2][nplane], n3);
+            const float2 un = padd(padd(n1, n2), n3);
+            float* const out = comp == 0 ? uxn : uzn;
+            out[g] = un.x;
+            if (up1) out[g1] = un.y;
         }
+        // second row on row NZ (outer frame): level 1 kept across the plane swap
+        if (in1 && !up1) { uxn[g1] = uxc[g1]; uzn[g1] = uzc[g1]; }
     }
 #undef SU
 #undef SM
-#undef GXI
-#undef VXI
-#undef GZI
-#undef VZI
+#undef GX
+#undef GZ
 }
 
 template <int NO>
@@ -894,7 +1040,8 @@ size_t step_smem_for(const StepArgs& a)
 }
 
 // Tile shapes and counts of the tiled kernel.  band_top: the fast path covers rows below
-// int_rows, so the interior tiles are flat kBandTZ x kBandTX tiles of the top band.  The
+// int_rows, so the interior tiles are flat tiles of the top band, all its rows (rounded up to
+// even, at most 16) by kBandTX columns.  The
 // absorbing layers are cut into tiles whose thickness divides npml evenly (at most kPmlTile)
 // and pml_run cells (kPmlRun when not tuned) along the layer.
 void plan_tiles(StepArgs& a, bool band_top, int pml_run)
@@ -903,7 +1050,7 @@ void plan_tiles(StepArgs& a, bool band_top, int pml_run)
     auto cdiv = [](int x, int y) { return (x + y - 1) / y; };
     const int nt = cdiv(a.npml, kPmlTile);
     const int th = cdiv(a.npml, nt);
-    a.tdz[0] = band_top ? kBandTZ : kTZ;
+    a.tdz[0] = band_top ? std::min((a.int_rows + 1) & ~1, 2 * kMaxOrder) : kTZ;
     a.tdx[0] = band_top ? kBandTX : kTX;
     a.tdz[1] = pml_run; a.tdx[1] = th;
     a.tdz[2] = th; a.tdx[2] = pml_run;

@@ -19,8 +19,7 @@ namespace fdfk {
 constexpr int kMaxOrder = 8;   // FD order 16 (the reference caps norder at (npml+1)/2)
 constexpr int kTZ = 32;        // default tile rows (z, the contiguous axis)
 constexpr int kTX = 32;        // default tile columns (x)
-constexpr int kBandTZ = 8;     // flat tiles of the top band (rows 1..2*norder) next to the fast path
-constexpr int kBandTX = 64;
+constexpr int kBandTX = 64;    // columns of the flat top-band tiles (rows 1..2*norder) next to the fast path
 constexpr int kPmlTile = 40;   // largest absorbing-layer thickness covered by one tile
 constexpr int kPmlRun = 24;    // absorbing-layer tile length along the layer
 constexpr int kThreads = 256;  // 8 warps per CTA
