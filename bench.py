@@ -352,8 +352,8 @@ def main():
     ap.add_argument("--no-fk-full", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--batch-events", type=int, default=64, help="config-3 events (0: skip batched and serving)")
-    ap.add_argument("--seq-sample", type=int, default=8, help="sequential solves timed for the comparison")
-    ap.add_argument("--serve-requests", type=int, default=192, help="config-5 requests (0: skip serving)")
+    ap.add_argument("--seq-sample", type=int, default=16, help="sequential solves timed for the comparison")
+    ap.add_argument("--serve-requests", type=int, default=2000, help="config-5 requests (0: skip serving)")
     ap.add_argument("--uneven-solves", type=int, default=24, help="config-4 solves (0: skip the uneven batch)")
     ap.add_argument("--uneven-seq-sample", type=int, default=4, help="config-4 solves timed one by one")
     args = ap.parse_args()
@@ -459,7 +459,7 @@ def main():
         se.seismogram_range(0, K, outx, outz)
         return se
 
-    solve_e2e().close()        # warm-up: module loading and this transform length's cuFFT plan
+    solve_e2e().close()        # warm-up: module loading and the first launches of every kernel
     barrier()
     t0 = time.perf_counter()
     se = solve_e2e()
@@ -477,7 +477,7 @@ def main():
     if rank == 0 and not args.no_fk_full:
         sf = F.Session(p, w["c"], stream=stream.cuda_stream)
         fkf, bazs_f, fl_f, fr_f = WL.fk_inputs(w)
-        sf.fk_background(fkf, bazs_f, fl_f, fr_f)          # warm-up (cuFFT plans, first touch)
+        sf.fk_background(fkf, bazs_f, fl_f, fr_f)          # warm-up (first launches, first touch)
         barrier()
         t0 = time.perf_counter()
         sf.fk_background(fkf, bazs_f, fl_f, fr_f)

@@ -284,9 +284,10 @@ __device__ void sample_receivers(const StepArgs& a, int blk)
         if ((((unsigned)(q < 32 ? st.z : st.w) >> (q & 31)) & 1u) == 0u) continue;
         const int ix = st.x - 3 + q / 7, iz = st.y - 3 + q % 7;
         const size_t g = gidx(a, iz, ix);
+        // explicit fused multiply-adds: the single-solve and batched copies of this code round alike
         const double wq = w[q];
-        sx += wq * (double)ux[g];
-        sz += wq * (double)uz[g];
+        sx = fma(wq, (double)ux[g], sx);
+        sz = fma(wq, (double)uz[g], sz);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -383,7 +384,7 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
     // Every load of a round is issued before the first shared-memory store, so a round costs one
     // memory latency.
     {
-        constexpr int kFill = 4;
+        constexpr int kFill = 2;
         const int P2 = T.UZ / 2, NP = P2 * T.UX;
         Walk wu(tid, P2, kThreads);   // (pair row, column) of this thread's items, in order
         for (int i0 = tid; i0 < NP; i0 += kFill * kThreads) {
@@ -410,7 +411,7 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                 }
             }
         }
-        constexpr int kFillM = 4;
+        constexpr int kFillM = 2;
         const int M2 = T.MZ / 2, NMP = M2 * T.MX;
         Walk wm(tid, M2, kThreads);
         for (int i0 = tid; i0 < NMP; i0 += kFillM * kThreads) {
