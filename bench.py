@@ -351,6 +351,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fk-full", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tuning", default="", help="SEG,RUN: the workload's launch shapes (fast-path segment "
+                    "columns, absorbing-layer run) given instead of autotuned")
     ap.add_argument("--batch-events", type=int, default=64, help="config-3 events (0: skip batched and serving)")
     ap.add_argument("--seq-sample", type=int, default=16, help="sequential solves timed for the comparison")
     ap.add_argument("--serve-requests", type=int, default=2000, help="config-5 requests (0: skip serving)")
@@ -408,7 +410,10 @@ def main():
     q = dict(p, nt=Wm + K - 1)
     fkp, bazs, fk_left, fk_right = WL.fk_inputs(dict(w, p=q))
     tuning = None
-    if not args.no_autotune:
+    if args.tuning:
+        seg, run = (int(v) for v in args.tuning.split(","))
+        tuning = {"seg_len": seg, "pml_run": run, "given": True}
+    elif not args.no_autotune:
         seg, run, ms_tuned = F.autotune(p, w["c"], steps=20)
         tuning = {"seg_len": seg, "pml_run": run, "ms_per_step_in_tuner": round(ms_tuned, 4)}
     sess = F.Session(q, w["c"], stream=stream.cuda_stream)
@@ -524,7 +529,8 @@ def main():
                              "whole_step_frac": round(step_equiv / peak, 4)},
                 "cpu_baseline": cpu, "clocks": clk}
         if tuning:
-            line["config"]["tuning"] = dict(tuning, note="launch shapes picked by fdfk_autotune")
+            line["config"]["tuning"] = dict(tuning, note="launch shapes given on the command line" if
+                                            tuning.get("given") else "launch shapes picked by fdfk_autotune")
         if extra:
             line.update(extra)
         if fk_ms is not None:
