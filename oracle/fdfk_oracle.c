@@ -17,8 +17,8 @@
  *    u + u_b(it) where u_b is added on the outer strips (Omega_II: the *_pml
  *    background strips); the PML operators act on u - u_b(it) where u_b is
  *    removed on the inner strips (Omega_I: the *_reg background strips).
- * 3. Free surface (top row iz = 1 when is_PML_top is false), stress image
- *    about the half row 1.5:
+ * 3. Free surface (top row iz = 1; applied in the PML-on-top mode too, item 5),
+ *    stress image about the half row 1.5:
  *      F_x(1) = dxx(l2m ux) + Dx[lam(1) (uz(2)-uz(1))/dz] + 2/dz * sxz(1.5)
  *      F_z(1) = dxx(mu uz)  + Dx[mu(1) (ux(2)-ux(1))/dz]  + 2/dz * szz(1.5)
  *      sxz(1.5) = H(mu1,mu2)(ux2-ux1)/dz + (mu1 Dx uz1 + mu2 Dx uz2)/2
@@ -38,8 +38,22 @@
  *    update does not divide the u1 forcing by (1 + dx dt) except on the free
  *    surface row; this is reproduced.
  *
- * The PML-on-top mode (is_PML_top) is not restated: the shipped step treats
- * the first interior row there in a way not yet pinned, so it returns -2.
+ * 5. PML on top (is_PML_top, izt = 1 - npml; pinned against the shipped step
+ *    on random state for norder 1..4 and 8, square and oblong cells):
+ *    - a fourth layer, rows izt+1..0 over every column but the outer frame
+ *      (the corners belong to it), damped in x and z like the bottom layer,
+ *      with the depth into it counted from row 1 (d' < 0), state in the top
+ *      arrays (bp*t*, bu*t); row izt is outer frame like row nz+npml;
+ *    - the interior update keeps the free-surface formula of item 3 on row 1
+ *      (the shipped step applies it whatever is_PML_top says); the absorbing
+ *      layers' row 1 uses the general split-field terms, and the right layer
+ *      leaves the u1 forcing undivided on every row;
+ *    - the absorbing layers' operator field is formed after the interior
+ *      update: where no inner strip lies (rows 1..nz-nbd, columns
+ *      nbd+1..nx-nbd) it holds the new u^{n+1}, elsewhere u^n minus the inner
+ *      strips.  Only the top layer's stencils reach those cells.
+ *    The FK background does not depend on izt (the shipped
+ *    comput_background_wavefield_ gives the same strips for both modes).
  */
 #include "fdfk_oracle.h"
 #include "fdfk_ops.h"
@@ -163,7 +177,8 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const real_t *c
                             const double *coef0, const double *coef1, real_t *ux, real_t *uz, real_t *const bp[12],
                             real_t *const bu[24])
 {
-    if (p->izt != 1) return -2;
+    const int top = p->izt != 1;   /* PML on top (item 5) */
+    if (top && p->izt != 1 - p->npml) return -2;
     if (p->norder < 1 || p->nbd != 2 * p->norder - 1 || p->npml < p->nbd || p->nz <= p->nbd || p->nx < 1) return -1;
     geo_t G = {p->nx, p->nz, p->npml, p->izt, p->nz + p->npml - p->izt + 1, p->nx + 2 * p->npml, p->norder, p->nbd};
     const geo_t *g = &G;
@@ -249,6 +264,21 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const real_t *c
         }
     }
 
+    if (top) {
+        /* item 5: the operator field of the layers, formed after the interior update */
+        for (size_t i = 0; i < n; ++i) { px[i] = ux[2 * i]; pz[i] = uz[2 * i]; }
+        apply_strips(p, g, it, strips, 0, 0, px);
+        apply_strips(p, g, it, strips, 1, 0, pz);
+        for (int ix = p->nbd + 1; ix <= nx - p->nbd; ++ix)
+            for (int iz = 1; iz <= nz - p->nbd; ++iz) {
+                size_t i = gi(g, iz, ix);
+                px[i] = nux1[i];
+                pz[i] = nuz1[i];
+            }
+        run_ops(p, 1, l2m, lam, mu, coef0, coef1, px, pz, pops);
+        for (size_t i = 0; i < n; ++i) { Sx[i] = px[i]; Sz[i] = pz[i]; }
+    }
+
     /* -------- PML update -------- */
     double logr = log(1.0 / p->R0);
     double d0x = (p->npower + 1) * (double)p->vpml * logr / (2.0 * npml * dx);
@@ -267,12 +297,13 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const real_t *c
         rz1[cc] = Sz[i1]; rz2[cc] = Sz[i2]; rx1[cc] = Sx[i1]; rx2[cc] = Sx[i2];
     }
 
-    /* sides: 0 = left, 1 = right, 2 = bottom */
-    for (int side = 0; side < 3; ++side) {
+    /* sides: 0 = left, 1 = right, 2 = bottom, 3 = top (item 5) */
+    for (int side = 0; side < (top ? 4 : 3); ++side) {
         int iz_lo, iz_hi, ix_lo, ix_hi;
         if (side == 0) { iz_lo = 1; iz_hi = nz; ix_lo = 2 - npml; ix_hi = 0; }
         else if (side == 1) { iz_lo = 1; iz_hi = nz; ix_lo = nx + 1; ix_hi = nx + npml - 1; }
-        else { iz_lo = nz + 1; iz_hi = nz + npml - 1; ix_lo = 2 - npml; ix_hi = nx + npml - 1; }
+        else if (side == 2) { iz_lo = nz + 1; iz_hi = nz + npml - 1; ix_lo = 2 - npml; ix_hi = nx + npml - 1; }
+        else { iz_lo = p->izt + 1; iz_hi = 0; ix_lo = 2 - npml; ix_hi = nx + npml - 1; }
 #pragma omp parallel for schedule(static)
         for (int ix = ix_lo; ix <= ix_hi; ++ix) {
             /* damping in x */
@@ -289,6 +320,9 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const real_t *c
                 if (side == 2) {
                     double s = (double)(iz - nz) * dz / Lz;
                     dzv = d0z * pow(s, npw); dzp = npw * d0z * pow(s, npw - 1) / Lz;
+                } else if (side == 3) {
+                    double s = (double)(1 - iz) * dz / Lz;
+                    dzv = d0z * pow(s, npw); dzp = -npw * d0z * pow(s, npw - 1) / Lz;
                 }
                 double yx = dxv * dt, yz = dzv * dt;
                 size_t i = gi(g, iz, ix);
@@ -297,10 +331,11 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const real_t *c
                 size_t ab, ap; /* bu index of level 1 (level 2 = +1), bp index */
                 if (side == 0) { ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - (1 - npml)); ab = 2 * ap; }
                 else if (side == 1) { ap = (size_t)(iz - 1) + (size_t)nz * (size_t)(ix - nx - 1); ab = 2 * ap; }
-                else { ap = (size_t)(iz - nz - 1) + (size_t)npml * (size_t)(ix - (1 - npml)); ab = 2 * ap; }
+                else if (side == 2) { ap = (size_t)(iz - nz - 1) + (size_t)npml * (size_t)(ix - (1 - npml)); ab = 2 * ap; }
+                else { ap = (size_t)(iz - (1 - npml)) + (size_t)npml * (size_t)(ix - (1 - npml)); ab = 2 * ap; }
                 for (int comp = 0; comp < 2; ++comp) {
                     double F1, F2, F3, S1, S3 = 0.0;
-                    if (iz == 1) {
+                    if (iz == 1 && !top) {
                         int cc = ix - (1 - npml);
                         size_t i1 = gi(g, 1, ix), i2 = gi(g, 2, ix);
                         if (comp == 0) {
@@ -321,23 +356,23 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const real_t *c
                         F2 = (double)pops[OP_ZX_LAM_Z][i] + (double)pops[OP_XZ_MU_Z][i];
                         F3 = pops[OP_Z2_MU_X][i];
                         S1 = (double)l2m[i] * cd1(g, coef1, Sx, iz, ix, 1, dx);
-                        if (side == 2) S3 = (double)mu[i] * cd1(g, coef1, Sx, iz, ix, 2, dz);
+                        if (side >= 2) S3 = (double)mu[i] * cd1(g, coef1, Sx, iz, ix, 2, dz);
                     } else {
                         F1 = pops[OP_X2_MU_Z][i];
                         F2 = (double)pops[OP_XZ_LAM_X][i] + (double)pops[OP_ZX_MU_X][i];
                         F3 = pops[OP_Z2_L2M_Z][i];
                         S1 = (double)mu[i] * cd1(g, coef1, Sz, iz, ix, 1, dx);
-                        if (side == 2) S3 = (double)l2m[i] * cd1(g, coef1, Sz, iz, ix, 2, dz);
+                        if (side >= 2) S3 = (double)l2m[i] * cd1(g, coef1, Sz, iz, ix, 2, dz);
                     }
-                    real_t *bpx = bp[side == 0 ? 0 + comp : side == 1 ? 2 + comp : 8 + 2 * comp];
-                    real_t *bpz = side == 2 ? bp[9 + 2 * comp] : NULL;
-                    int base = (side == 0 ? 0 : side == 1 ? 6 : 12) + 3 * comp;
+                    real_t *bpx = bp[side == 0 ? 0 + comp : side == 1 ? 2 + comp : side == 2 ? 8 + 2 * comp : 4 + 2 * comp];
+                    real_t *bpz = side == 2 ? bp[9 + 2 * comp] : side == 3 ? bp[5 + 2 * comp] : NULL;
+                    int base = (side == 0 ? 0 : side == 1 ? 6 : side == 2 ? 12 : 18) + 3 * comp;
                     real_t *b1 = bu[base], *b2 = bu[base + 1], *b3 = bu[base + 2];
                     double Px = bpx[ap];
                     double Pxn = ((1.0 - yx / 2) * Px - dt * dxp * S1) / (1.0 + yx / 2);
                     double u1 = b1[ab], u1m = b1[ab + 1];
                     double n1;
-                    if (side == 1 && iz != 1)
+                    if (side == 1 && (top || iz != 1))
                         n1 = ((2.0 - yx * yx) * u1 - (1.0 - yx) * u1m) / (1.0 + yx) + k * (F1 + (Pxn + Px) / 2.0);
                     else
                         n1 = ((2.0 - yx * yx) * u1 - (1.0 - yx) * u1m + k * (F1 + (Pxn + Px) / 2.0)) / (1.0 + yx);
@@ -366,7 +401,7 @@ int fdfk_oracle_updatedispl(const fdfk_oracle_params *p, int it, const real_t *c
 
     /* -------- commit levels for every updated cell -------- */
     for (int ix = 2 - npml; ix <= nx + npml - 1; ++ix)
-        for (int iz = 1; iz <= nz + npml - 1; ++iz) {
+        for (int iz = top ? p->izt + 1 : 1; iz <= nz + npml - 1; ++iz) {
             size_t i = gi(g, iz, ix);
             ux[2 * i + 1] = ux[2 * i]; ux[2 * i] = nux1[i];
             uz[2 * i + 1] = uz[2 * i]; uz[2 * i] = nuz1[i];
@@ -381,9 +416,9 @@ int fdfk_oracle_simulate(const fdfk_oracle_params *p, const real_t *const strips
                          const real_t *rx, const real_t *rz, real_t x0, real_t z0, int nstp, int nsis,
                          real_t *seisx, real_t *seisz, int steps_limit)
 {
-    if (p->izt != 1) return -2;
+    if (p->izt != 1 && p->izt != 1 - p->npml) return -2;
     int nx = p->nx, nz = p->nz, npml = p->npml, norder = p->norder;
-    size_t n = (size_t)(nz + npml) * (size_t)(nx + 2 * npml);
+    size_t n = (size_t)(nz + npml - p->izt + 1) * (size_t)(nx + 2 * npml);
     real_t *ux = (real_t *)calloc(2 * n, sizeof(real_t)), *uz = (real_t *)calloc(2 * n, sizeof(real_t));
     size_t side = (size_t)nz * npml, tb = (size_t)npml * (nx + 2 * npml);
     real_t *bpbuf = (real_t *)calloc(4 * side + 8 * tb, sizeof(real_t));

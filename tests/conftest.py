@@ -13,6 +13,8 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 STEP_CASES = ("n3", "n1", "n8", "n3_minpml_aniso", "n2_odd")
+# the PML-on-top mode (is_PML_top, izt = 1 - npml)
+STEP_CASES_TOP = ("top_n1", "top_n2", "top_n3")
 
 
 def pytest_configure(config):

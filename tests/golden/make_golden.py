@@ -9,7 +9,8 @@ Fixtures:
 
 * ``step_<name>.npz`` - one call of the shipped ``updatedispl_`` on seeded
   random state (wavefield, PML split fields, memory variables, background
-  strips) and heterogeneous material: inputs and outputs.
+  strips) and heterogeneous material: inputs and outputs (``step_top_*``: the
+  PML-on-top mode, izt = 1 - npml).
 * ``loop_layered.npz`` - the time loop of src/FDFK2D.f90:465-532 driven by the
   shipped ``updatedispl_`` and ``loadseis`` restated from src/Submain.f90:33-116,
   with background strips from the shipped ``comput_background_wavefield_``
@@ -53,12 +54,14 @@ def material(rng, NZ, NX, hetero=True):
     return c
 
 
-def step_case(name, seed, nx, nz, npml, norder, dx=200.0, dz=200.0, dt=0.01):
+def step_case(name, seed, nx, nz, npml, norder, dx=200.0, dz=200.0, dt=0.01, top=False):
+    """top: the PML-on-top mode (is_PML_top, izt = 1 - npml: npml more rows above row 1)."""
     rng = np.random.default_rng(seed)
     nbd = 2 * norder - 1
-    NZ, NX = nz + npml, nx + 2 * npml
+    izt = 1 - npml if top else 1
+    NZ, NX = nz + npml - izt + 1, nx + 2 * npml
     nt = 0
-    p = dict(norder=norder, nx=nx, nz=nz, npml=npml, izt=1, is_PML_top=False, npower=2, nbd=nbd, nt=nt,
+    p = dict(norder=norder, nx=nx, nz=nz, npml=npml, izt=izt, is_PML_top=top, npower=2, nbd=nbd, nt=nt,
              dx=dx, dz=dz, dt=dt, R0=1e-3)
     c = material(rng, NZ, NX)
     p["vpml"] = float(np.sqrt((c[1] + 2 * c[2]) / c[0]).max())
@@ -176,6 +179,10 @@ if __name__ == "__main__":
     step_case("n8", 13, nx=40, nz=30, npml=16, norder=8)
     step_case("n3_minpml_aniso", 14, nx=20, nz=14, npml=5, norder=3, dx=250.0, dz=125.0)
     step_case("n2_odd", 15, nx=17, nz=11, npml=7, norder=2, dx=150.0, dz=175.0, dt=0.008)
+    # PML on top
+    step_case("top_n2", 16, nx=20, nz=14, npml=6, norder=2, top=True)
+    step_case("top_n3", 17, nx=26, nz=18, npml=8, norder=3, dx=250.0, dz=200.0, top=True)
+    step_case("top_n1", 18, nx=15, nz=9, npml=3, norder=1, dx=180.0, dz=220.0, dt=0.008, top=True)
     loop_case()
     # P from the right (cos of the mean back-azimuth > 0), grid offset
     fk_case("p_ramp", True, 0.07e-3, (-25.0, 20.0), 2.0, 120, 0.01, x0=-1500.0, z0=0.0)

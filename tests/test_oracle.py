@@ -3,7 +3,7 @@ shipped libraries, plus its pure-formula parts against known values."""
 import numpy as np
 import pytest
 
-from conftest import STEP_CASES, load_npz, max_rel, rel_l2, step_inputs
+from conftest import STEP_CASES, STEP_CASES_TOP, load_npz, max_rel, rel_l2, step_inputs
 
 # One restated step vs one shipped step: float32 state, the restatement forms
 # sums in double where the shipped code rounds intermediates to float.
@@ -27,7 +27,7 @@ def test_fd_coefficients_order6(oracle_lib):
     assert c0[2, 0] == 0.0 and c1[2, 1] == 0.0
 
 
-@pytest.mark.parametrize("name", STEP_CASES)
+@pytest.mark.parametrize("name", STEP_CASES + STEP_CASES_TOP)
 def test_oracle_step_matches_shipped(oracle_lib, name):
     d = load_npz("step_" + name)
     p, strips, c, c0, c1, ux, uz, bp, bu = step_inputs(d)
@@ -53,12 +53,26 @@ def test_oracle_time_loop_matches_shipped(oracle_lib):
         assert rel_l2(sz[:, r], d["seisz"][:, r]) < LOOP_TOL
 
 
-def test_oracle_rejects_pml_top(oracle_lib):
+def test_oracle_rejects_other_top_rows(oracle_lib):
+    """izt is 1 (free surface) or 1 - npml (PML on top); anything else is an error."""
     d = load_npz("step_n1")
     p, strips, c, c0, c1, ux, uz, bp, bu = step_inputs(d)
-    p["izt"] = 1 - p["npml"]
+    p["izt"] = 0
     with pytest.raises(RuntimeError):
         oracle_lib.updatedispl(p, strips, c, c0, c1, ux, uz, bp, bu, 0)
+
+
+def test_oracle_top_mode_differs_from_free_surface(oracle_lib):
+    """The PML-on-top fixtures are not the free-surface step of the same arrays: run as izt = 1 on
+    the rows below the top layer they disagree (the top layer's cells feed rows 1..2 norder)."""
+    d = load_npz("step_top_n2")
+    p, strips, c, c0, c1, ux, uz, bp, bu = step_inputs(d)
+    npml = p["npml"]
+    q = dict(p, izt=1, is_PML_top=False)
+    cut = lambda a: np.asfortranarray(a[..., npml:, :]) if a.ndim == 3 else np.asfortranarray(a[npml:, :])
+    ux1, uz1, c1_ = cut(ux), cut(uz), cut(c)
+    oracle_lib.updatedispl(q, strips, c1_, c0, c1, ux1, uz1, bp, bu, 0)
+    assert max_rel(ux1[0], d["out_ux"][0, npml:, :]) > 1e-3
 
 
 def test_zero_state_zero_background_stays_zero(oracle_lib):
