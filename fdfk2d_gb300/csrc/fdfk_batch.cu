@@ -245,6 +245,9 @@ int fdfk_batch_add(fdfk_batch* b, fdfk_session* s)
     if (!b || !s) return set_error(FDFK_EINVAL, "NULL argument");
     if (s->batch) return set_error(FDFK_ESTATE, "the session already belongs to a batch");
     if (s->p.norder != b->norder) return set_error(FDFK_EINVAL, "the session's norder differs from the batch's");
+    if (s->izt != 1)
+        return set_error(FDFK_EUNSUPPORTED, "a session with the absorbing layer on top steps alone (its top layer "
+                                            "needs a launch after the interior update)");
     for (int t = s->it; t <= s->p.nt; ++t)
         if (!s->have_bg[t]) return set_error(FDFK_ESTATE, "the session has no background for time index " + std::to_string(t));
     int rc = pull(b);

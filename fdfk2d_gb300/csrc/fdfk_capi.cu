@@ -118,7 +118,6 @@ namespace {
 int validate(const fdfk_params* p)
 {
     if (!p) return fail(FDFK_EINVAL, "params is NULL");
-    if (p->is_PML_top) return fail(FDFK_EUNSUPPORTED, "is_PML_top: only the free-surface top boundary is implemented");
     if (p->norder < 1 || p->norder > kMaxOrder) return fail(FDFK_EINVAL, "norder must be 1..8");
     if (p->nbd != 2 * p->norder - 1) return fail(FDFK_EINVAL, "nbd must equal 2*norder-1");
     if (p->npml < p->nbd) return fail(FDFK_EINVAL, "npml must be >= 2*norder-1");
@@ -127,7 +126,8 @@ int validate(const fdfk_params* p)
     if (p->nt < 0) return fail(FDFK_EINVAL, "nt must be >= 0");
     if (!(p->dx > 0.f) || !(p->dz > 0.f) || !(p->dt > 0.0)) return fail(FDFK_EINVAL, "dx, dz, dt must be positive");
     if (!(p->R0 > 0.0) || !(p->R0 < 1.0)) return fail(FDFK_EINVAL, "R0 must be in (0, 1)");
-    if ((double)(p->nz + p->npml) * (p->nx + 2 * p->npml) > 2.0e9) return fail(FDFK_EINVAL, "grid too large");
+    if ((double)(p->nz + (p->is_PML_top ? 2 : 1) * p->npml) * (p->nx + 2 * p->npml) > 2.0e9)
+        return fail(FDFK_EINVAL, "grid too large");
     return FDFK_OK;
 }
 
@@ -175,7 +175,7 @@ cudaError_t ensure_coefficients()
 // stream uses them yet; otherwise the upload first waits for the session's stream.
 int upload_material(fdfk_session* s, const float* c, bool fresh)
 {
-    const size_t nc = 3 * (size_t)s->NZ * s->NX;
+    const size_t nc = 3 * (size_t)s->rows * s->NX;
     int lo = 0, hi = 0;
     cudaStream_t up = nullptr;
     cudaEvent_t done = nullptr;
@@ -191,7 +191,8 @@ int upload_material(fdfk_session* s, const float* c, bool fresh)
     if (e == cudaSuccess) e = cudaMemsetAsync(d_flag, 0, sizeof(int), up);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_c, c, nc * sizeof(float), cudaMemcpyHostToDevice, up);
     if (e == cudaSuccess)
-        e = launch_material(d_c, s->NZ, s->NX, s->ldz, s->p.dt * s->p.dt, s->kdt2, s->lam, s->mu, d_flag, up);
+        e = launch_material(d_c, s->rows, s->NX, s->ldz, s->p.dt * s->p.dt, s->kdt2, s->lam, s->mu, d_flag, up,
+                            s->izt - s->zorg);
     int flag = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, up);
     if (d_c) cudaFreeAsync(d_c, up);
@@ -214,7 +215,10 @@ int upload_material(fdfk_session* s, const float* c, bool fresh)
 // whole cells from the interface (first PML cell s = h), L = npml*h.
 void damping(const fdfk_params& p, std::vector<DampCol>& dx, std::vector<DampCol>& dz)
 {
-    const int NX = p.nx + 2 * p.npml, NZ = p.nz + p.npml;
+    // dz: rows izt..nz+npml (izt = 1 - npml with the absorbing layer on top: its depth counted
+    // from row 1 upwards, d' < 0)
+    const int izt = p.is_PML_top ? 1 - p.npml : 1;
+    const int NX = p.nx + 2 * p.npml, NZ = p.nz + p.npml - izt + 1;
     const double lg = std::log(1.0 / p.R0);
     const double Lx = (double)p.npml * p.dx, Lz = (double)p.npml * p.dz;
     const double d0x = (p.npower + 1) * (double)p.vpml * lg / (2.0 * Lx);
@@ -231,11 +235,13 @@ void damping(const fdfk_params& p, std::vector<DampCol>& dx, std::vector<DampCol
         dx[c] = make_damp((float)(d * p.dt), (float)(sg * dp * p.dt));
     }
     for (int r = 0; r < NZ; ++r) {
-        int iz = r + 1;
-        if (iz <= p.nz) continue;
-        double s = (double)(iz - p.nz) * p.dz / Lz;
+        int iz = r + izt;
+        double s = 0.0, sg = 0.0;
+        if (iz <= 0) { s = (double)(1 - iz) * p.dz / Lz; sg = -1.0; }
+        else if (iz > p.nz) { s = (double)(iz - p.nz) * p.dz / Lz; sg = 1.0; }
+        else continue;
         double d = d0z * std::pow(s, p.npower), dp = p.npower * d0z * std::pow(s, p.npower - 1) / Lz;
-        dz[r] = make_damp((float)(d * p.dt), (float)(dp * p.dt));
+        dz[r] = make_damp((float)(d * p.dt), (float)(sg * dp * p.dt));
     }
 }
 
@@ -291,10 +297,13 @@ int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out
     s->p = *p;
     s->NZ = p->nz + p->npml;
     s->NX = p->nx + 2 * p->npml;
+    s->izt = p->is_PML_top ? 1 - p->npml : 1;
+    s->zorg = plane_zorg(s->izt);
+    s->rows = s->NZ - s->izt + 1;
     // FDFK_TILED_ONLY=1 keeps every cell on the tiled kernel (used to cross-check the two paths).
     const char* tiled_only = std::getenv("FDFK_TILED_ONLY");
     const bool march = p->norder <= kMarchMaxOrder && p->nz >= 2 * p->norder + 1 && !(tiled_only && tiled_only[0] == '1');
-    s->ldz = plane_ldz(p->nz, p->npml, p->norder, march);
+    s->ldz = plane_ldz(p->nz, p->npml, p->norder, march, s->izt);
     const size_t n = (size_t)s->ldz * s->NX;
 
     auto alloc = [&](void** ptr, size_t bytes) -> int {
@@ -310,12 +319,13 @@ int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out
     AL(s->mu, n * sizeof(float));
     for (int l = 0; l < 2; ++l) { AL(s->ux[l], n * sizeof(float)); AL(s->uz[l], n * sizeof(float)); }
     if (march) { AL(s->fux, n * sizeof(float)); AL(s->fuz, n * sizeof(float)); }
-    for (int k = 0; k < 18; ++k)          // l, r, b (the top PML is not used with a free surface)
+    const int nbu = p->is_PML_top ? 24 : 18;   // l, r, b, and t with the absorbing layer on top
+    for (int k = 0; k < nbu; ++k)
         for (int l = 0; l < 2; ++l) AL(s->bu[k][l], bu_elems(*p, k) * sizeof(float));
     for (int k = 0; k < 12; ++k)
-        if (k < 4 || k >= 8) AL(s->bp[k], bp_elems(*p, k) * sizeof(float));
+        if (k < 4 || k >= 8 || p->is_PML_top) AL(s->bp[k], bp_elems(*p, k) * sizeof(float));
     AL(s->dampx, s->NX * sizeof(DampCol));
-    AL(s->dampz, s->NZ * sizeof(DampCol));
+    AL(s->dampz, s->rows * sizeof(DampCol));
     for (int k = 0; k < NSTRIP; ++k) AL(s->strip[k], strip_elems(*p, k) * (size_t)(p->nt + 1) * sizeof(float));
 #undef AL
     s->have_bg.assign(p->nt + 1, 0);
@@ -338,6 +348,7 @@ int fdfk_session_create(const fdfk_params* p, const float* c, fdfk_session** out
     StepArgs& a = s->base;
     a.nx = p->nx; a.nz = p->nz; a.npml = p->npml; a.norder = p->norder; a.nbd = p->nbd;
     a.NZ = s->NZ; a.NX = s->NX; a.ldz = s->ldz;
+    a.izt = s->izt; a.zorg = s->zorg;
     a.dx = p->dx; a.dz = p->dz;
     a.dx2r = (float)(1.0 / (double)(p->dx * p->dx));
     a.dx2p = 1.0f / (p->dx * p->dx);
@@ -507,6 +518,12 @@ int fdfk_session_advance(fdfk_session* s, int nsteps)
             if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("step launch: ") + cudaGetErrorString(e));
             g_launches.fetch_add(1);
         }
+        if (s->izt != 1) {
+            // the top absorbing layer after the interior update, whose new values it reads
+            cudaError_t e = launch_step_top(a, s->stream);
+            if (e != cudaSuccess) return fail(FDFK_ECUDA, std::string("top-layer launch: ") + cudaGetErrorString(e));
+            g_launches.fetch_add(1);
+        }
         s->cur ^= 1;
         s->it += 1;
     }
@@ -568,6 +585,10 @@ int fdfk_session_advance_timed(fdfk_session* s, int nsteps, int sample_every, fl
             cudaEventRecord(s->join, s->side);
             cudaStreamWaitEvent(s->stream, s->join, 0);
         }
+        if (r == cudaSuccess && s->izt != 1) {   // the top absorbing layer after the interior update
+            r = launch_step_top(a, s->stream);
+            nl += 1;
+        }
         if (r != cudaSuccess) { cleanup(); return fail(FDFK_ECUDA, std::string("launch: ") + cudaGetErrorString(r)); }
         g_launches.fetch_add(nl + (two ? 2 : 0));
         s->cur ^= 1;
@@ -596,7 +617,7 @@ int fdfk_session_advance_timed(fdfk_session* s, int nsteps, int sample_every, fl
 int fdfk_session_interior_cells(const fdfk_session* s, long long* interior, long long* edge)
 {
     if (!s || !interior || !edge) return fail(FDFK_EINVAL, "NULL argument");
-    const long long total = (long long)s->NZ * s->NX;
+    const long long total = (long long)s->rows * s->NX;
     *interior = s->march.n_bands > 0 ? (long long)(s->p.nz - 2 * s->p.norder) * s->p.nx : 0;
     *edge = total - *interior;
     return FDFK_OK;
@@ -657,9 +678,10 @@ int fdfk_session_upload_state(fdfk_session* s, const float* ux, const float* uz,
     const size_t n = (size_t)s->ldz * s->NX;
     std::vector<float> lv[4];
     for (auto& v : lv) v.assign(n, 0.f);
+    const int zoff = s->izt - s->zorg;   // plane row of grid row izt
     for (int x = 0; x < s->NX; ++x)
-        for (int z = 0; z < s->NZ; ++z) {
-            size_t src = 2 * ((size_t)z + (size_t)s->NZ * x), dst = (size_t)z + (size_t)s->ldz * x;
+        for (int z = 0; z < s->rows; ++z) {
+            size_t src = 2 * ((size_t)z + (size_t)s->rows * x), dst = (size_t)(z + zoff) + (size_t)s->ldz * x;
             lv[0][dst] = ux[src]; lv[1][dst] = ux[src + 1];
             lv[2][dst] = uz[src]; lv[3][dst] = uz[src + 1];
         }
@@ -708,12 +730,13 @@ int fdfk_session_download_state(fdfk_session* s, float* ux, float* uz, float* co
     CK(cudaMemcpyAsync(lv[3].data(), s->uz[o], n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     const int npml = s->p.npml, nx = s->p.nx;
+    const int zoff = s->izt - s->zorg;   // plane row of grid row izt
     for (int x = 0; x < s->NX; ++x)
-        for (int z = 0; z < s->NZ; ++z) {
-            size_t dst = 2 * ((size_t)z + (size_t)s->NZ * x), src = (size_t)z + (size_t)s->ldz * x;
-            const int ix = x + 1 - npml, iz = z + 1;
+        for (int z = 0; z < s->rows; ++z) {
+            size_t dst = 2 * ((size_t)z + (size_t)s->rows * x), src = (size_t)(z + zoff) + (size_t)s->ldz * x;
+            const int ix = x + 1 - npml, iz = z + s->izt;
             // the outer frame is never advanced: its level 2 is left as the caller holds it
-            const bool frame = ix == 1 - npml || ix == nx + npml || iz == s->NZ;
+            const bool frame = ix == 1 - npml || ix == nx + npml || iz == s->NZ || (s->izt != 1 && iz == s->izt);
             ux[dst] = lv[0][src];
             uz[dst] = lv[2][src];
             if (!frame) { ux[dst + 1] = lv[1][src]; uz[dst + 1] = lv[3][src]; }
@@ -739,7 +762,7 @@ int fdfk_session_download_state(fdfk_session* s, float* ux, float* uz, float* co
             for (int r = 0; r < n1; ++r) {
                 bool frame;
                 if (sidearr) frame = (k < 6) ? j == 0 : j == npml - 1;
-                else frame = r == npml - 1 || j == 0 || j == s->NX - 1;
+                else frame = (k < 18 ? r == npml - 1 : r == 0) || j == 0 || j == s->NX - 1;   // b / t
                 if (frame) continue;
                 const size_t i = (size_t)r + (size_t)n1 * j;
                 bu[k][2 * i] = pl[0][i];
@@ -872,7 +895,7 @@ int fdfk_session_snapshot(fdfk_session* s, float* ux, float* uz)
     }
     // level 2 = the plane not holding u^n; rows 1..nz of columns 1..nx
     const int o = s->cur ^ 1;
-    const size_t first = (size_t)s->ldz * s->p.npml;
+    const size_t first = (size_t)s->ldz * s->p.npml + (size_t)(1 - s->zorg);
     const size_t pitch = (size_t)s->ldz * sizeof(float);
     CK(cudaMemcpy2DAsync(ux, s->p.nz * sizeof(float), s->ux[o] + first, pitch, s->p.nz * sizeof(float), s->p.nx,
                          cudaMemcpyDeviceToHost, s->stream));
@@ -913,7 +936,9 @@ static int fk_job(const fdfk_fk_params* p, const double* bazs, int nll, const fl
                   const float* fkr, FkJob& J)
 {
     if (!p || !bazs || !fkl || !fkr) return fail(FDFK_EINVAL, "NULL argument");
-    if (p->izt != 1) return fail(FDFK_EUNSUPPORTED, "FK background: only izt = 1 (free surface on top) is implemented");
+    // the strips do not depend on izt (the grid's top row): the shipped library gives the same
+    // background for the free-surface and the absorbing-layer-on-top modes
+    if (p->izt > 1 || p->izt < 1 - p->npml) return fail(FDFK_EINVAL, "FK: izt must be 1 or 1 - npml");
     if (p->nx < 1 || p->nbd < 1 || p->nz <= p->nbd || p->npml < p->nbd || p->nt < 1 || !(p->dt > 0.0) ||
         !(p->dx > 0.f) || !(p->dz > 0.f))
         return fail(FDFK_EINVAL, "FK: need nx >= 1, nz > nbd >= 1, npml >= nbd, nt >= 1 and positive dt, dx, dz");
@@ -1103,7 +1128,7 @@ void updatedispl_(const int* norder, const int* nx, const int* nz, const int* np
         std::fprintf(stderr, "fdfk_gb300 updatedispl_: %s (%s)\n", what, g_err.c_str());
         std::abort();
     };
-    if (*izt != 1 || p.is_PML_top) { g_err = "is_PML_top"; die("only the free-surface top boundary is implemented"); }
+    if (*izt != (p.is_PML_top ? 1 - p.npml : 1)) { g_err = "izt"; die("izt must be 1, or 1 - npml with is_PML_top"); }
     if (p.norder < 1 || p.norder > kMaxOrder) { g_err = "norder"; die("stencil order outside 1..8"); }
     if (!caller_coefficients_match(p.norder, coef0, coef1)) {
         g_err = "coef0/coef1";

@@ -94,7 +94,7 @@ __device__ __forceinline__ void march_ring(const StepArgs& a, const MarchArgs& m
     const float rdx = 1.0f / a.dx, rdz = 1.0f / a.dz;
     const float dx2 = a.dx2r, dz2 = a.dz2;
 
-    const int rowoff = r0 - 1;
+    const int rowoff = r0 - a.zorg;   // even: r0 is odd and 1 - zorg is even
     auto gofs = [&](int ix) -> int { return (ix + npml - 1) * ldz + rowoff; };
     float* const ringA = ring + 2 * lane;
     float* const ringB = ring + 64 * RG::kSlotsA * RG::kFieldsA + 2 * lane;

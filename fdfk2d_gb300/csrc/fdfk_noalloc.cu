@@ -68,12 +68,12 @@ struct DeintTab {
 };
 
 __global__ void na_material(const float* __restrict__ c, int NZ, int NX, int ldz, double dt2, float* __restrict__ kd,
-                            float* __restrict__ la, float* __restrict__ mu, int* __restrict__ flag)
+                            float* __restrict__ la, float* __restrict__ mu, int* __restrict__ flag, int zpad)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long long)ldz * NX) return;
-    const int z = (int)(i % ldz), x = (int)(i / ldz);
-    if (z >= NZ) {
+    const int z = (int)(i % ldz) - zpad, x = (int)(i / ldz);
+    if (z < 0 || z >= NZ) {
         kd[i] = 0.f;
         la[i] = 0.f;
         mu[i] = 1.f;
@@ -161,10 +161,10 @@ __global__ void na_pack_bu(DeintTab t, int npml, int NX)
     } while (0)
 
 cudaError_t launch_material(const float* c, int NZ, int NX, int ldz, double dt2, float* kd, float* la, float* mu,
-                            int* flag, cudaStream_t st)
+                            int* flag, cudaStream_t st, int zpad)
 {
     const long long n = (long long)ldz * NX;
-    na_material<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(c, NZ, NX, ldz, dt2, kd, la, mu, flag);
+    na_material<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(c, NZ, NX, ldz, dt2, kd, la, mu, flag, zpad);
     return cudaGetLastError();
 }
 
@@ -187,6 +187,10 @@ size_t noalloc_floats_needed(const fdfk_params& p)
 int step_noalloc(const fdfk_params& p, int it, const float* const strips[12], const float* c, float* ux, float* uz,
                  float* const bp[12], float* const bu[24], cudaStream_t st, std::string& err, long long* launches)
 {
+    if (p.is_PML_top) {
+        err = "the allocation-free step implements the free-surface top boundary only";
+        return FDFK_EUNSUPPORTED;
+    }
     const int NZ = p.nz + p.npml, NX = p.nx + 2 * p.npml, ldz = (NZ + 31) / 32 * 32;
     const size_t n = (size_t)ldz * NX;
     const size_t need = noalloc_floats_needed(p);
@@ -314,6 +318,7 @@ int step_noalloc(const fdfk_params& p, int it, const float* const strips[12], co
     StepArgs a{};
     a.nx = p.nx; a.nz = p.nz; a.npml = p.npml; a.norder = p.norder; a.nbd = p.nbd;
     a.NZ = NZ; a.NX = NX; a.ldz = ldz;
+    a.izt = 1; a.zorg = 1;
     a.dx = p.dx; a.dz = p.dz;
     a.dx2r = (float)(1.0 / (double)(p.dx * p.dx));
     a.dx2p = 1.0f / (p.dx * p.dx);

@@ -24,10 +24,10 @@ int step_noalloc(const fdfk_params& p, int it, const float* const strips[12], co
                  float* const bp[12], float* const bu[24], cudaStream_t st, std::string& err, long long* launches);
 
 // Material planes from the reference's material array c(3, NZ, NX) (rho, lambda, mu) on the
-// device: dt^2/rho, lambda, mu with leading dimension ldz (rows NZ..ldz-1 padding: 0, 0, 1).  Sets
-// bit 0 of *flag where rho <= 0 and bit 1 where mu <= 0 or lambda + 2 mu <= 0 (the checks of the
-// session API).  Enqueued on st.
+// device: dt^2/rho, lambda, mu with leading dimension ldz, row r of c at plane row r + zpad (plane
+// rows before zpad and from zpad + NZ on are padding: 0, 0, 1).  Sets bit 0 of *flag where rho <= 0
+// and bit 1 where mu <= 0 or lambda + 2 mu <= 0 (the checks of the session API).  Enqueued on st.
 cudaError_t launch_material(const float* c, int NZ, int NX, int ldz, double dt2, float* kd, float* la, float* mu,
-                            int* flag, cudaStream_t st);
+                            int* flag, cudaStream_t st, int zpad = 0);
 
 }  // namespace fdfk

@@ -98,12 +98,15 @@ long long fdfk_session_device_bytes(const fdfk_params* p, int nrcv, int nsis)
 {
     if (!p || p->nx < 1 || p->nz < 1 || p->npml < 0 || p->nt < 0 || nrcv < 0) return -1;
     const bool fast = p->norder <= kMarchMaxOrder && p->nz >= 2 * p->norder + 1;
-    const long long NZ = p->nz + p->npml, NX = p->nx + 2LL * p->npml, ldz = plane_ldz(p->nz, p->npml, p->norder, fast);
+    const int izt = p->is_PML_top ? 1 - p->npml : 1;
+    const long long NZ = p->nz + p->npml - izt + 1, NX = p->nx + 2LL * p->npml;
+    const long long ldz = plane_ldz(p->nz, p->npml, p->norder, fast, izt);
     const long long n = ldz * NX;
     const long long side = (long long)p->nz * p->npml, tb = (long long)p->npml * NX;
     const long long nx = p->nx, nz = p->nz, nbd = p->nbd;
     const long long strips = 4 * (nz - nbd) * nbd + 2 * nbd * nx + 4 * nz * nbd + 2 * nbd * (nx + 2 * nbd);
-    long long f = (fast ? 9 : 7) * n + 2 * (12 * side + 6 * tb) + 4 * side + 4 * tb + strips * (p->nt + 1LL);
+    const long long ntb = p->is_PML_top ? 2 : 1;   // bottom, and top layer arrays
+    long long f = (fast ? 9 : 7) * n + 2 * (12 * side + 6 * ntb * tb) + 4 * side + 4 * ntb * tb + strips * (p->nt + 1LL);
     f += 2LL * nrcv + (nrcv > 0 ? 2LL * (nsis + 1) * nrcv : 0);
     return 4 * f + (long long)sizeof(DampCol) * (NX + NZ);
 }
@@ -132,6 +135,7 @@ int fdfk_server_submit(fdfk_server* sv, const fdfk_solve_request* r, long long* 
 {
     if (!sv || !r || !id) return set_error(FDFK_EINVAL, "NULL argument");
     if (r->p.norder != sv->norder) return set_error(FDFK_EINVAL, "the request's norder differs from the server's");
+    if (r->p.is_PML_top) return set_error(FDFK_EUNSUPPORTED, "requests with the absorbing layer on top are solved alone");
     if (!r->c || !r->bazs || !r->fk_left || !r->fk_right || !r->seisx || !r->seisz || r->nrcv < 1 || r->nsis < 0)
         return set_error(FDFK_EINVAL, "request: missing inputs or outputs");
     Req* q = new (std::nothrow) Req();

@@ -12,7 +12,10 @@ struct fdfk_batch;
 
 struct fdfk_session {
     fdfk_params p{};
-    int NZ = 0, NX = 0, ldz = 0;
+    int NZ = 0, NX = 0, ldz = 0;   // last row nz + npml, columns, plane leading dimension
+    int izt = 1;                   // top row: 1 (free surface) or 1 - npml (absorbing layer on top)
+    int zorg = 1;                  // grid row at plane row 0 (plane_zorg(izt))
+    int rows = 0;                  // grid rows izt..NZ (the reference arrays' first extent)
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;     // second stream for the tiled kernel
     cudaEvent_t fork = nullptr, join = nullptr;

@@ -63,8 +63,8 @@ __host__ __device__ __forceinline__ TileDims tile_dims(int NO, int TZ, int TX)
 }
 
 struct Rect {
-    int side;       // 0 interior, 1 left PML, 2 right PML, 3 bottom PML
-    int cls;        // tile class (StepArgs::tdz / tdx): 0 interior, 1 side PML, 2 bottom PML
+    int side;       // 0 interior, 1 left PML, 2 right PML, 3 bottom PML, 4 top PML
+    int cls;        // tile class (StepArgs::tdz / tdx): 0 interior, 1 side PML, 2 bottom and top PML
     int z0, x0;     // first row / column of the tile
     int zlo, zhi, xlo, xhi;  // output rectangle (inclusive)
 };
@@ -119,12 +119,12 @@ __device__ __forceinline__ int ordx(const StepArgs& a, int ix, int NO)
 }
 __device__ __forceinline__ int ordz(const StepArgs& a, int iz, int NO)
 {
-    int n = min(min(iz - 1, a.nz + a.npml - iz), NO);
+    int n = min(min(iz - a.izt, a.nz + a.npml - iz), NO);
     return n < 0 ? 0 : n;
 }
 __device__ __forceinline__ size_t gidx(const StepArgs& a, int iz, int ix)
 {
-    return (size_t)(iz - 1) + (size_t)(ix + a.npml - 1) * (size_t)a.ldz;
+    return (size_t)(iz - a.zorg) + (size_t)(ix + a.npml - 1) * (size_t)a.ldz;
 }
 
 // Address of the background at (iz, ix) on the outer strips (Omega_II): the x component,
@@ -178,6 +178,15 @@ __device__ __forceinline__ StripRect strip_rect(const StepArgs& a, bool inner, i
 __device__ __forceinline__ Rect decode_tile(const StepArgs& a, int b)
 {
     Rect r;
+    if (a.top_pass) {   // the top layer: rows izt+1..0 (row izt is outer frame), every column
+        r.side = 4;
+        r.cls = 2;
+        r.zlo = a.izt + 1; r.zhi = 0; r.xlo = 1 - a.npml; r.xhi = a.nx + a.npml;
+        int q, m;
+        divmod_small(b, a.tiles_t_z, q, m);
+        r.z0 = r.zlo + m * a.tdz[2]; r.x0 = r.xlo + q * a.tdx[2];
+        return r;
+    }
     int ni = a.tiles_int_z * a.tiles_int_x;
     int nl = a.tiles_l_z * a.tiles_l_x;
     if (b < ni) {
@@ -231,8 +240,8 @@ __device__ __forceinline__ double delta_weight(double x)
 // in the model (bit q of the masks: point q = 7 * (column offset + 3) + row offset + 3) and each
 // point's FP64 weight; formed once when the receivers are set.  Block r, 64 threads: thread q < 49
 // forms point q.
-__global__ void receiver_sites_kernel(int nrcv, int nx, int nz, int npml, float dx, float dz, float x0, float z0,
-                                      const float* __restrict__ rxs, const float* __restrict__ rzs,
+__global__ void receiver_sites_kernel(int nrcv, int nx, int nz, int npml, int izt, float dx, float dz, float x0,
+                                      float z0, const float* __restrict__ rxs, const float* __restrict__ rzs,
                                       int4* __restrict__ site, double* __restrict__ wout)
 {
     const int r = blockIdx.x, q = threadIdx.x;
@@ -241,7 +250,7 @@ __global__ void receiver_sites_kernel(int nrcv, int nx, int nz, int npml, float 
     const int irx = (int)floorf((rx - x0) / dx) + 1;
     const int irz = (int)floorf((rz - z0) / dz) + 1;
     const int xlo = max(1 - npml, irx - 3), xhi = min(nx + npml, irx + 3);
-    const int zlo = max(1, irz - 3), zhi = min(nz + npml, irz + 3);
+    const int zlo = max(izt, irz - 3), zhi = min(nz + npml, irz + 3);
     const int ix = irx - 3 + q / 7, iz = irz - 3 + q % 7;
     const bool in = q < 49 && ix >= xlo && ix <= xhi && iz >= zlo && iz <= zhi;
     double w = 0.0;
@@ -263,7 +272,7 @@ cudaError_t launch_receiver_sites(const StepArgs& a, int nrcv, float x0, float z
                                   const float* rz, int4* site, double* w, cudaStream_t s)
 {
     if (nrcv <= 0) return cudaSuccess;
-    receiver_sites_kernel<<<nrcv, 64, 0, s>>>(nrcv, a.nx, a.nz, a.npml, a.dx, a.dz, x0, z0, rx, rz, site, w);
+    receiver_sites_kernel<<<nrcv, 64, 0, s>>>(nrcv, a.nx, a.nz, a.npml, a.izt, a.dx, a.dz, x0, z0, rx, rz, site, w);
     return cudaGetLastError();
 }
 
@@ -379,11 +388,17 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
     const float rdx = 1.0f / a.dx, rdz = 1.0f / a.dz;
     const float* uxc = a.ux[a.cur];
     const float* uzc = a.uz[a.cur];
+    const int izt = a.izt;
 
     // ---- phase 0: field tile and material tile, by row pairs; then the background strips -----
     // Every load of a round is issued before the first shared-memory store, so a round costs one
-    // memory latency.
+    // memory latency.  The top layer's launch reads the interior cells that no inner strip covers
+    // (rows 1..nz-nbd, columns nbd+1..nx-nbd) at u^{n+1}, from the plane the step has just written:
+    // the reference forms the absorbing layers' operator field after its interior update.
     {
+        const float* const uxq = a.top_pass ? a.ux[a.cur ^ 1] : uxc;
+        const float* const uzq = a.top_pass ? a.uz[a.cur ^ 1] : uzc;
+        const int qz1 = nz - a.nbd, qx0 = a.nbd + 1, qx1 = nx - a.nbd;
         constexpr int kFill = 2;
         const int P2 = T.UZ / 2, NP = P2 * T.UX;
         Walk wu(tid, P2, kThreads);   // (pair row, column) of this thread's items, in order
@@ -397,9 +412,18 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                 vx[q] = f2s(0.f);
                 vz[q] = f2s(0.f);
                 if (i < NP && ix >= 1 - npml && ix <= nx + npml) {
-                    const long long g = (long long)(iz - 1) + (long long)(ix + npml - 1) * a.ldz;
-                    if (iz >= 1 && iz <= NZ) { vx[q].x = uxc[g]; vz[q].x = uzc[g]; }
-                    if (iz + 1 >= 1 && iz + 1 <= NZ) { vx[q].y = uxc[g + 1]; vz[q].y = uzc[g + 1]; }
+                    const long long g = (long long)(iz - a.zorg) + (long long)(ix + npml - 1) * a.ldz;
+                    const bool qc = ix >= qx0 && ix <= qx1;
+                    if (iz >= izt && iz <= NZ) {
+                        const bool nw = qc && iz >= 1 && iz <= qz1;
+                        vx[q].x = (nw ? uxq : uxc)[g];
+                        vz[q].x = (nw ? uzq : uzc)[g];
+                    }
+                    if (iz + 1 >= izt && iz + 1 <= NZ) {
+                        const bool nw = qc && iz + 1 >= 1 && iz + 1 <= qz1;
+                        vx[q].y = (nw ? uxq : uxc)[g + 1];
+                        vz[q].y = (nw ? uzq : uzc)[g + 1];
+                    }
                 }
             }
 #pragma unroll
@@ -423,9 +447,9 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                 wm.next();
                 l[q] = f2s(0.f); m[q] = f2s(1.f);
                 if (i < NMP && ix >= 1 - npml && ix <= nx + npml) {
-                    const long long g = (long long)(iz - 1) + (long long)(ix + npml - 1) * a.ldz;
-                    if (iz >= 1 && iz <= NZ) { l[q].x = __ldg(a.lam + g); m[q].x = __ldg(a.mu + g); }
-                    if (iz + 1 >= 1 && iz + 1 <= NZ) { l[q].y = __ldg(a.lam + g + 1); m[q].y = __ldg(a.mu + g + 1); }
+                    const long long g = (long long)(iz - a.zorg) + (long long)(ix + npml - 1) * a.ldz;
+                    if (iz >= izt && iz <= NZ) { l[q].x = __ldg(a.lam + g); m[q].x = __ldg(a.mu + g); }
+                    if (iz + 1 >= izt && iz + 1 <= NZ) { l[q].y = __ldg(a.lam + g + 1); m[q].y = __ldg(a.mu + g + 1); }
                 }
             }
 #pragma unroll
@@ -560,13 +584,14 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                     dzz = pfma(c, f2(__fsub_rn(wz[OM + k], wz[OM - k]), __fsub_rn(wz[OM + 1 + k], wz[OM + 1 - k])), dzz);
                     dzx = pfma(c, f2(__fsub_rn(wx[OM + k], wx[OM - k]), __fsub_rn(wx[OM + 1 + k], wx[OM + 1 - k])), dzx);
                 }
-                // diffzx_reg forms v on rows 2..nz; diffzx_pml on rows 2..NZ-1, columns 2-npml..nx+npml-1
+                // diffzx_reg forms v on rows 2..nz; diffzx_pml on rows izt+1..NZ-1, columns
+                // 2-npml..nx+npml-1 (the regular block it leaves out is read by no layer cell)
                 const bool colv = pml ? (ix >= 2 - npml && ix <= nx + npml - 1) : (ix >= 1 - NO && ix <= nx + NO);
-                const int zmax = pml ? NZ - 1 : nz;
+                const int zmin = pml ? izt + 1 : 2, zmax = pml ? NZ - 1 : nz;
                 float2 a1 = pmul(pmul(lds2(SM(sLam, z, x)), dzz), f2s(rdz));
                 float2 a4 = pmul(pmul(lds2(SM(sMu, z, x)), dzx), f2s(rdz));
-                if (!(colv && iz >= 2 && iz <= zmax)) { a1.x = 0.f; a4.x = 0.f; }
-                if (!(colv && iz + 1 >= 2 && iz + 1 <= zmax)) { a1.y = 0.f; a4.y = 0.f; }
+                if (!(colv && iz >= zmin && iz <= zmax)) { a1.x = 0.f; a4.x = 0.f; }
+                if (!(colv && iz + 1 >= zmin && iz + 1 <= zmax)) { a1.y = 0.f; a4.y = 0.f; }
                 sts2(v1 + o, a1);
                 sts2(v4 + o, a4);
             }
@@ -616,13 +641,18 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                     dxz = pfma(c, psub(lds2(SU(suz, L, x + k)), lds2(SU(suz, L, x - k))), dxz);
                     dxx = pfma(c, psub(lds2(SU(sux, L, x + k)), lds2(SU(sux, L, x - k))), dxx);
                 }
-                // diffxz_reg forms v on rows 1..nz+norder, columns 1..nx; diffxz_pml on rows 1..NZ-1
+                // diffxz_reg forms v on rows 1..nz+norder, columns 1..nx; diffxz_pml on rows izt..NZ-1
+                // except the regular block rows 1..nz-norder x columns 1..nx (which the top layer reads)
                 const bool colv = pml ? (ix >= 2 - npml && ix <= nx + npml - 1) : (ix >= 1 && ix <= nx);
-                const int zmax = pml ? NZ - 1 : nz + NO;
+                const int zmin = pml ? izt : 1, zmax = pml ? NZ - 1 : nz + NO;
+                const bool blk = pml && ix >= 1 && ix <= nx;
                 float2 a2 = pmul(pmul(lds2(SM(sMu, L, x)), dxz), f2s(rdx));
                 float2 a3 = pmul(pmul(lds2(SM(sLam, L, x)), dxx), f2s(rdx));
-                if (!(colv && iz >= 1 && iz <= zmax)) { a2.x = 0.f; a3.x = 0.f; }
-                if (!(colv && iz + 1 >= 1 && iz + 1 <= zmax)) { a2.y = 0.f; a3.y = 0.f; }
+                if (!(colv && iz >= zmin && iz <= zmax) || (blk && iz >= 1 && iz <= nz - NO)) { a2.x = 0.f; a3.x = 0.f; }
+                if (!(colv && iz + 1 >= zmin && iz + 1 <= zmax) || (blk && iz + 1 >= 1 && iz + 1 <= nz - NO)) {
+                    a2.y = 0.f;
+                    a3.y = 0.f;
+                }
                 sts2(v2 + o, a2);
                 sts2(v3 + o, a3);
             }
@@ -647,7 +677,7 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         // never stored)
         if (ix < R.xlo || ix > R.xhi || iz > R.zhi) continue;
         const bool in1 = z + 1 < TZ && iz + 1 <= R.zhi;
-        const long long g = (long long)(iz - 1) + (long long)(ix + npml - 1) * a.ldz;
+        const long long g = (long long)(iz - a.zorg) + (long long)(ix + npml - 1) * a.ldz;
         const long long g1 = in1 ? g + 1 : g;
 
         if (pml && (ix == 1 - npml || ix == nx + npml || iz == NZ)) {
@@ -663,8 +693,8 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         const int nz0 = ordz(a, iz, NO), nz1 = ordz(a, iz + 1, NO);
         // every column ix-NO..ix (row iz-NO..iz) has the full order: no reduced-order half points
         const bool fullx = ix - NO >= NO - npml + 1 && ix <= nx + npml - NO;
-        const bool fullz0 = iz - NO >= NO + 1 && iz <= NZ - NO;
-        const bool fullz1 = iz + 1 - NO >= NO + 1 && iz + 1 <= NZ - NO;
+        const bool fullz0 = iz - NO >= NO + izt && iz <= NZ - NO;
+        const bool fullz1 = iz + 1 - NO >= NO + izt && iz + 1 <= NZ - NO;
         const float2 kd = f2(__ldg(a.kdt2 + g), __ldg(a.kdt2 + g1));
 
         // x-direction second derivatives dxx(l2m ux), dxx(mu uz)
@@ -772,12 +802,15 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         // ---- absorbing-layer cells: split-field update ----------------------------------
         const int side = R.side;
         const bool up1 = in1 && iz + 1 != NZ;   // row NZ is outer frame
+        // bottom (3) and top (4) layers: damped in x and z, both memory variables
+        const bool zl = side >= 3;
         long long ap;   // state index of row iz (row iz+1: ap + 1)
         if (side == 1) ap = (long long)(iz - 1) + (long long)nz * (ix - (1 - npml));
         else if (side == 2) ap = (long long)(iz - 1) + (long long)nz * (ix - nx - 1);
-        else ap = (long long)(iz - nz - 1) + (long long)npml * (ix - (1 - npml));
-        const int base = side == 1 ? 0 : side == 2 ? 6 : 12;
-        const int bpx0 = side == 1 ? 0 : side == 2 ? 2 : 8;
+        else if (side == 3) ap = (long long)(iz - nz - 1) + (long long)npml * (ix - (1 - npml));
+        else ap = (long long)(iz - izt) + (long long)npml * (ix - (1 - npml));
+        const int base = side == 1 ? 0 : side == 2 ? 6 : side == 3 ? 12 : 18;
+        const int bpx0 = side == 1 ? 0 : side == 2 ? 2 : side == 3 ? 8 : 4;
         const int nplane = a.cur ^ 1;
         const long long ap1 = up1 ? ap + 1 : ap;
         auto ld = [&](const float* p) { return f2(p[ap], p[ap1]); };
@@ -808,16 +841,16 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
 
         const DampCol dxc = a.dampx[ix + npml - 1];
         DampCol dzc0{0.f, 0.f, 1.f, 1.f}, dzc1{0.f, 0.f, 1.f, 1.f};
-        if (side == 3) {
-            dzc0 = a.dampz[iz - 1];
-            dzc1 = a.dampz[iz + 1 <= NZ ? iz : iz - 1];
+        if (zl) {
+            dzc0 = a.dampz[iz - izt];
+            dzc1 = a.dampz[iz + 1 <= NZ ? iz + 1 - izt : iz - izt];
         }
         const float2 yx = f2s(dxc.y), yz = f2(dzc0.y, dzc1.y);
         // split 2: (2 - yx yz) u - (1 - (yx + yz)/2) u^{n-1}, over 1 + (yx + yz)/2
         const float2 hs = pmul(f2s(0.5f), padd(yx, yz));
         const float2 A2 = pfma(f2s(-dxc.y), yz, f2s(2.0f));
         const float2 B2 = psub(f2s(1.0f), hs);
-        const float2 r2 = side == 3 ? f2(fast_rcp(__fadd_rn(1.0f, hs.x)), fast_rcp(__fadd_rn(1.0f, hs.y))) : f2s(dxc.rh);
+        const float2 r2 = zl ? f2(fast_rcp(__fadd_rn(1.0f, hs.x)), fast_rcp(__fadd_rn(1.0f, hs.y))) : f2s(dxc.rh);
         // split 1 (x damping): (2 - yx^2) u - (1 - yx) u^{n-1}
         const float2 A1 = f2s(fmaf(-dxc.y, dxc.y, 2.0f)), B1 = f2s(__fsub_rn(1.0f, dxc.y));
         const float2 Cx = f2s(__fsub_rn(1.0f, __fmul_rn(0.5f, dxc.y)));   // 1 - yx/2
@@ -837,11 +870,13 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                 S1 = pmul(mu0, dxuz);
                 S3 = pmul(l2m0, dzuz);
             }
-            if (iz == 1) {   // free-surface row of a side layer (first row of the pair)
+            // free-surface row of a side layer (first row of the pair; with the top layer, row 1
+            // of the side layers takes the general terms)
+            if (iz == 1 && izt == 1) {
                 F2.x = sFS[(comp == 0 ? kFsF2x : kFsF2z) * TX + x];
                 F3.x = sFS[(comp == 0 ? kFsF3x : kFsF3z) * TX + x];
             }
-            float* bpx = a.bp[side == 3 ? bpx0 + 2 * comp : bpx0 + comp];
+            float* bpx = a.bp[zl ? bpx0 + 2 * comp : bpx0 + comp];
             const float2 Px = ld(bpx);
             // memory variable: ((1 - yx/2) Px - dt d' S1) / (1 + yx/2)
             const float2 Pxn = pmul(pfma(f2s(-dxc.dtdp), S1, pmul(Cx, Px)), f2s(dxc.rh));
@@ -852,14 +887,14 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             const float2 t1 = pfma(A1, u1, pmul(f2s(-B1.x), u1m));
             const float2 n1o = pmul(padd(t1, f1), f2s(dxc.r1));
             float2 n1 = n1o;
-            if (side == 2) {   // right layer below row 1: the force is not divided by 1 + yx
+            if (side == 2) {   // right layer below a free-surface row 1: the force is not divided by 1 + yx
                 const float2 n1r = pfma(t1, f2s(dxc.r1), f1);
-                n1 = f2(iz == 1 ? n1o.x : n1r.x, n1r.y);
+                n1 = f2(iz == 1 && izt == 1 ? n1o.x : n1r.x, n1r.y);
             }
             const float2 n2 = pmul(pfma(kd, F2, pfma(A2, u2, pmul(f2(-B2.x, -B2.y), u2m))), r2);
             float2 n3;
-            if (side == 3) {
-                float* bpz = a.bp[9 + 2 * comp];
+            if (zl) {
+                float* bpz = a.bp[bpx0 + 1 + 2 * comp];
                 const float2 Pz = ld(bpz);
                 const float2 Cz = f2(__fsub_rn(1.0f, __fmul_rn(0.5f, dzc0.y)), __fsub_rn(1.0f, __fmul_rn(0.5f, dzc1.y)));
                 const float2 Pzn = pmul(pfma(f2(-dzc0.dtdp, -dzc1.dtdp), S3, pmul(Cz, Pz)), f2(dzc0.rh, dzc1.rh));
@@ -882,6 +917,16 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         }
         // second row on row NZ (outer frame): level 1 kept across the plane swap
         if (in1 && !up1) { uxn[g1] = uxc[g1]; uzn[g1] = uzc[g1]; }
+    }
+    // the top layer's outer row izt (never advanced): level 1 kept, by the tiles next to it
+    if (R.side == 4 && R.z0 == izt + 1) {
+        for (int x = tid; x < TX; x += kThreads) {
+            const int ix = R.x0 + x;
+            if (ix > R.xhi) break;
+            const long long g = (long long)(izt - a.zorg) + (long long)(ix + npml - 1) * a.ldz;
+            uxn[g] = uxc[g];
+            uzn[g] = uzc[g];
+        }
     }
 #undef SU
 #undef SM
@@ -963,6 +1008,7 @@ __global__ void fdfk_batch_bump(BatchTab t)
 template <int NO>
 static cudaError_t launch_no(const StepArgs& a, int n_sample_blocks, cudaStream_t s)
 {
+    // (a.top_pass: a.n_tiles counts the top layer's tiles, no receiver blocks)
     static int configured = 0;   // dynamic shared memory opted in so far (bytes)
     size_t smem = 0;
     for (int c = 0; c < 3; ++c)
@@ -979,6 +1025,26 @@ static cudaError_t launch_no(const StepArgs& a, int n_sample_blocks, cudaStream_
 
 // Receiver-sampling blocks appended to a tiled launch (one warp per receiver).
 int sample_blocks(int nrcv) { return nrcv > 0 ? (nrcv + kThreads / 32 - 1) / (kThreads / 32) : 0; }
+
+cudaError_t launch_step_top(const StepArgs& a0, cudaStream_t s)
+{
+    if (a0.izt == 1) return cudaSuccess;
+    StepArgs a = a0;
+    a.top_pass = 1;
+    a.n_tiles = a.tiles_t_z * a.tiles_t_x;
+    a.nrcv = 0;
+    switch (a.norder) {
+    case 1: return launch_no<1>(a, 0, s);
+    case 2: return launch_no<2>(a, 0, s);
+    case 3: return launch_no<3>(a, 0, s);
+    case 4: return launch_no<4>(a, 0, s);
+    case 5: return launch_no<5>(a, 0, s);
+    case 6: return launch_no<6>(a, 0, s);
+    case 7: return launch_no<7>(a, 0, s);
+    case 8: return launch_no<8>(a, 0, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
 
 cudaError_t launch_step(const StepArgs& a, cudaStream_t s)
 {
@@ -1061,6 +1127,10 @@ void plan_tiles(StepArgs& a, bool band_top, int pml_run)
     a.tiles_l_x = cdiv(a.npml, a.tdx[1]);
     a.tiles_b_z = cdiv(a.npml, a.tdz[2]);
     a.tiles_b_x = cdiv(a.NX, a.tdx[2]);
+    // the top layer (rows izt+1..0) in the bottom tiles' shape, launched on its own (launch_step_top)
+    a.tiles_t_z = a.izt < 1 ? cdiv(-a.izt, a.tdz[2]) : 0;
+    a.tiles_t_x = a.izt < 1 ? a.tiles_b_x : 0;
+    a.top_pass = 0;
     a.n_tiles = a.tiles_int_z * a.tiles_int_x + 2 * a.tiles_l_z * a.tiles_l_x + a.tiles_b_z * a.tiles_b_x;
 }
 

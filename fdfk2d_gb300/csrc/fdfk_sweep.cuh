@@ -42,9 +42,12 @@ inline DampCol make_damp(float y, float dtdp)
 }
 
 struct StepArgs {
-    // geometry (izt = 1, free surface on top)
+    // geometry: rows izt..NZ (izt = 1: free surface on top; izt = 1 - npml: absorbing layer on
+    // top), columns 1-npml..nx+npml; plane row 0 holds grid row zorg (zorg = izt, or izt - 1 so
+    // that row 1 sits at an even plane row: the fast path's 8-byte row pairs stay aligned)
     int nx, nz, npml, norder, nbd;
-    int NZ, NX, ldz;          // rows, columns, leading dimension (>= NZ, padded)
+    int NZ, NX, ldz;          // last row (nz + npml), columns, leading dimension (padded)
+    int izt, zorg;
     float dx, dz;
     float dx2r, dx2p, dz2;    // 1/(dx*dx) as the regular (double-rounded) and PML (float) operators form it
     float dt;
@@ -70,7 +73,9 @@ struct StepArgs {
     int tiles_int_z, tiles_int_x;       // interior tiling
     int tiles_l_z, tiles_l_x;           // left / right PML tiling (same shape)
     int tiles_b_z, tiles_b_x;           // bottom PML tiling
-    int n_tiles;
+    int tiles_t_z, tiles_t_x;           // top PML tiling (izt < 1; rows izt+1..0, the bottom tiles' shape)
+    int top_pass;                       // 1: this launch is the top layer's (after the interior update)
+    int n_tiles;                        // tiles of this launch (the top layer's alone when top_pass)
     int tdz[3], tdx[3];                 // tile rows / columns of the interior, side-PML and bottom-PML tiles
     // receivers sampled in the same launch (0 when this step takes no sample)
     int nrcv;
@@ -96,7 +101,7 @@ struct MarchArgs {
     int n_segs;
 };
 
-// Tile shapes and counts of fdfk_step_kernel for a (fdfk_sweep.cu); needs nx, nz, npml, NX, int_rows.
+// Tile shapes and counts of fdfk_step_kernel for a (fdfk_sweep.cu); needs nx, nz, npml, NX, izt, int_rows.
 void plan_tiles(StepArgs& a, bool band_top, int pml_run = kPmlRun);
 
 // Dynamic shared memory of a's tiled launch.
@@ -128,19 +133,27 @@ struct BatchTab {
 };
 
 cudaError_t launch_step_batch(const BatchTab& t, int norder, int blocks, size_t smem, cudaStream_t s);
+// The top absorbing layer's launch of one solve (izt < 1): after the interior update of the step,
+// whose new values the layer's operator field reads (a with top_pass set by the call).
+cudaError_t launch_step_top(const StepArgs& a, cudaStream_t s);
 cudaError_t launch_batch_bump(const BatchTab& t, cudaStream_t s);
 // Frame (frame_blocks blocks) and fast path (blocks blocks) of a batch step.
 cudaError_t launch_march_batch(const BatchTab& t, int norder, int frame_blocks, int blocks, cudaStream_t s);
 // Blocks of one solve's frame launch (the kernel that writes StepArgs::fux / fuz before the fast path).
 int frame_blocks(const StepArgs& a);
 
-// Leading dimension of the planar arrays: NZ rows, or more when the fast path runs, whose last
-// 64-row band may reach past NZ (nz + 63 - 2*norder rows); the extra rows are padding (u = 0,
-// lambda = 0, mu = 1, dt^2/rho = 0), rounded to 32 rows.
-inline int plane_ldz(int nz, int npml, int norder, bool fast_path)
+// First plane row of a grid with top row izt: izt itself when 1 - izt is even, else one padding
+// row above it (the fast path loads rows in 8-byte pairs starting at odd grid rows).
+inline int plane_zorg(int izt) { return ((1 - izt) & 1) ? izt - 1 : izt; }
+
+// Leading dimension of the planar arrays: rows zorg..nz+npml, or more when the fast path runs, whose
+// last 64-row band may reach past nz + npml (to row nz + 63 - 2*norder); the extra rows are
+// padding (u = 0, lambda = 0, mu = 1, dt^2/rho = 0), rounded to 32 rows.
+inline int plane_ldz(int nz, int npml, int norder, bool fast_path, int izt = 1)
 {
-    int need = nz + npml;
-    if (fast_path && nz + 64 - 2 * norder > need) need = nz + 64 - 2 * norder;
+    const int zorg = plane_zorg(izt);
+    int need = nz + npml - zorg + 1;
+    if (fast_path && nz + 65 - 2 * norder - zorg > need) need = nz + 65 - 2 * norder - zorg;
     return (need + 31) / 32 * 32;
 }
 

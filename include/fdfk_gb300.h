@@ -10,7 +10,8 @@
  * the calling thread.
  *
  * Grid conventions (src/FDFK2D.f90:125, src/Input.f90:177-183):
- *   NZ = nz + npml rows (iz = 1..nz+npml, free surface on top: izt = 1)
+ *   NZ = nz + npml - izt + 1 rows (iz = izt..nz+npml; izt = 1 with a free surface
+ *   on top, izt = 1 - npml with the absorbing layer on top, is_PML_top)
  *   NX = nx + 2*npml columns (ix = 1-npml..nx+npml)
  *   c(1:3, NZ, NX) = rho, lambda, mu
  *   ux, uz (1:2, NZ, NX): level 1 = u^n, level 2 = u^{n-1}
@@ -38,7 +39,8 @@ typedef struct fdfk_params {
     int norder;     /* half FD order, 1..8 */
     int nx, nz;     /* interior grid */
     int npml;       /* absorbing-layer width in cells (>= 2*norder-1) */
-    int is_PML_top; /* reference logical; only 0 (free surface) is implemented */
+    int is_PML_top; /* reference logical: 0 free surface on top (izt = 1), 1 absorbing layer on top
+                       (izt = 1 - npml: npml more rows above row 1; sessions step alone, not in batches) */
     int npower;     /* damping profile exponent (reference: 2) */
     int nbd;        /* background-strip width, 2*norder-1 */
     int nt;         /* last time index; strips hold nt+1 samples */

@@ -51,9 +51,11 @@ def test_library_loads_and_validates_without_gpu(built):
         with pytest.raises(F.FDFKError) as e:
             F.Session(p, c)
         assert e.value.code == -1, change
-    with pytest.raises(F.FDFKError) as e:
-        F.Session(dict(base, is_PML_top=True), c)
-    assert e.value.code == -2
+    # the absorbing layer on top is validated the same way (npml rows more above row 1)
+    for change in (dict(npml=4), dict(nz=5)):
+        with pytest.raises(F.FDFKError) as e:
+            F.Session(dict(base, is_PML_top=True, **change), np.ones((3, 40, 56), np.float32, order="F"))
+        assert e.value.code == -1, change
 
 
 def test_shapes_match_reference_allocations():
@@ -70,9 +72,11 @@ def test_fk_entry_points_validate_without_gpu(built):
     p = dict(nx=16, nz=12, npml=6, nbd=3, nt=50, dt=0.01, dx=250.0, dz=250.0, ds=1e-3, f0=2.0, rayp=6e-5)
     m = np.array([[0.0], [6000.0], [3500.0], [2700.0]], np.float32)
     baz = np.zeros(16 + 12)
-    with pytest.raises(F.FDFKError) as e:
-        F.fk_background(dict(p, izt=2), baz, m, m)
-    assert e.value.code == -2
+    # the grid's top row is 1 (free surface) or 1 - npml (absorbing layer on top)
+    for izt in (2, -6):
+        with pytest.raises(F.FDFKError) as e:
+            F.fk_background(dict(p, izt=izt), baz, m, m)
+        assert e.value.code == -1, izt
     for change in (dict(nbd=7), dict(nz=3), dict(nt=0), dict(dt=0.0), dict(nx=0)):
         with pytest.raises((F.FDFKError, ValueError)) as e:
             F.fk_background(dict(p, **change), np.zeros(int(dict(p, **change)["nx"]) + 12), m, m)
