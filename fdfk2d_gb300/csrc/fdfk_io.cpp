@@ -432,12 +432,13 @@ int fdfk_run(const char* inpath, const char* inparfile, const char* outpath, con
         }
     } g{&in};
     const std::string dir = inpath, out = outpath ? outpath : ".", name = fsis && *fsis ? fsis : "seis";
-    if (in.is_PML_top) return set_error(FDFK_EUNSUPPORTED, "is_PML_top: only the free-surface top boundary is implemented");
-    const int NX = in.nx + 2 * in.npml, NZ = in.nz + in.npml;
+    // rows izt..nz+npml (izt = 1 - npml with the absorbing layer on top)
+    const int NX = in.nx + 2 * in.npml, NZ = in.nz + in.npml - in.izt + 1;
 
-    // stability (src/Submain.f90:118-164) and the absorbing-layer constants (src/FDFK2D.f90:407-421)
+    // stability (src/Submain.f90:118-164, every cell of c) and the absorbing-layer constants
+    // (src/FDFK2D.f90:407-421)
     double dt_stable = 0.0;
-    if ((rc = fdfk_stable_dt(in.norder, in.nx, in.nz, in.npml, in.dx, in.dz, in.c, &dt_stable))) return rc;
+    if ((rc = fdfk_stable_dt(in.norder, in.nx, NZ - in.npml, in.npml, in.dx, in.dz, in.c, &dt_stable))) return rc;
     if (in.dt > dt_stable)
         return fail("The dt is too large to stablize the simulation ! The stable dt = " + std::to_string(dt_stable) +
                     " is recommended");
@@ -466,13 +467,14 @@ int fdfk_run(const char* inpath, const char* inparfile, const char* outpath, con
                              "a 2-D simulation of the teleseismic wavefield is inaccurate\n");
 
     fdfk_params p{};
-    p.norder = in.norder; p.nx = in.nx; p.nz = in.nz; p.npml = in.npml; p.is_PML_top = 0; p.npower = 2;
+    p.norder = in.norder; p.nx = in.nx; p.nz = in.nz; p.npml = in.npml; p.is_PML_top = in.is_PML_top ? 1 : 0;
+    p.npower = 2;
     p.nbd = 2 * in.norder - 1; p.nt = nt; p.dx = in.dx; p.dz = in.dz; p.dt = in.dt; p.vpml = vpml; p.R0 = 1e-3;
     if ((rc = fdfk_session_create(&p, in.c, &g.s))) return rc;
     double rayp = in.rayp;
     if (std::fabs(rayp) < 1e-9) rayp = rayp < 0.0 ? -1e-9 : 1e-9;   // src/FDFK2D.f90:428
     fdfk_fk_params fk{};
-    fk.nx = in.nx; fk.nz = in.nz; fk.npml = in.npml; fk.izt = 1; fk.nbd = p.nbd; fk.nt = nt; fk.src_type = in.src_type;
+    fk.nx = in.nx; fk.nz = in.nz; fk.npml = in.npml; fk.izt = in.izt; fk.nbd = p.nbd; fk.nt = nt; fk.src_type = in.src_type;
     fk.x0 = in.x0; fk.z0 = in.z0; fk.dx = in.dx; fk.dz = in.dz; fk.dt = in.dt; fk.ds = in.ds; fk.f0 = in.f0;
     fk.rayp = rayp;
     if ((rc = fdfk_session_fk_background(g.s, &fk, bazs.data(), in.nlayer_left, in.fk_left, in.nlayer_right,

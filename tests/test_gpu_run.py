@@ -1,7 +1,7 @@
 """GPU: program FDFK2D through fdfk_run - the reference's input folder in, SU seismograms out -
 against the oracle pipeline on the same inputs (FK restatement, restated time loop, profile
 geometry restated in oracle/geodesy_oracle.py, radial projection).  Besides a small folder of this
-suite's own, the reference's examples test2 (order 6, P) and test1 (order 16 -> norder 8, S) run
+suite's own (with the free surface and with the absorbing layer on top), the reference's examples test2 (order 6, P) and test1 (order 16 -> norder 8, S) run
 with a shortened record and their receivers moved down to where the incident wave arrives within it."""
 import os
 
@@ -38,7 +38,7 @@ def _oracle_pipeline(F, oracle_lib, inp):
     c = d["c"]
     vpml = float(np.sqrt((c[1] + 2 * c[2]) / c[0]).max())
     p = dict(norder=d["norder"], nx=nx, nz=nz, npml=npml, nbd=2 * d["norder"] - 1, nt=nt, dx=d["dx"], dz=d["dz"],
-             dt=dt, vpml=vpml, npower=2, R0=1e-3, izt=1)
+             dt=dt, vpml=vpml, npower=2, R0=1e-3, izt=int(d["izt"]))
     coordx = (np.float32(d["x0"]) + (np.arange(1 - npml, nx + npml + 1) - 1).astype(np.float32) * np.float32(d["dx"]))
     bazs = geodesy_oracle.profile_bazs(d["lat_org"], d["lon_org"], d["az_org"], d["evla"], d["evlo"], coordx)
     fp = dict(nx=nx, nz=nz, npml=npml, nbd=p["nbd"], nt=nt, dt=dt, dx=d["dx"], dz=d["dz"], f0=d["f0"], ds=d["ds"],
@@ -50,9 +50,10 @@ def _oracle_pipeline(F, oracle_lib, inp):
     return sx, sz, nsis, np.float32(nstp * dt)
 
 
-def test_run_matches_oracle_pipeline(F, oracle_lib, tmp_path):
+@pytest.mark.parametrize("pml_top", [False, True])
+def test_run_matches_oracle_pipeline(F, oracle_lib, tmp_path, pml_top):
     inp, out = str(tmp_path / "in"), str(tmp_path / "out")
-    write_folder(inp)
+    write_folder(inp, pml_top=pml_top)
     os.makedirs(out)
     F.run(inp, "inpar.dat", out, "seis")
     ox, oz, nsis, tstp = _oracle_pipeline(F, oracle_lib, inp)
