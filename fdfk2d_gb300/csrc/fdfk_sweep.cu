@@ -390,23 +390,80 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
     const float* uzc = a.uz[a.cur];
     const int izt = a.izt;
 
-    // ---- phase 0: field tile and material tile, by row pairs; then the background strips -----
-    // Every load of a round is issued before the first shared-memory store, so a round costs one
-    // memory latency.  The top layer's launch reads the interior cells that no inner strip covers
-    // (rows 1..nz-nbd, columns nbd+1..nx-nbd) at u^{n+1}, from the plane the step has just written:
-    // the reference forms the absorbing layers' operator field after its interior update.
+    // ---- phase 0: field tile and material tile, by row pairs, and the background strips ------
+    // One round of loads covers (for tiles up to kU * 256 field pairs and kM * 256 material
+    // pairs) the whole tile: the field, the material and the strip values that meet the field
+    // tile are all in flight before the first shared-memory store, so the phase costs one memory
+    // latency.  The strips are added (regular field) or removed (absorbing layers' operator
+    // field) after a barrier, in place: one rounding per value, as u + b / u - b.  The top layer's
+    // launch reads the interior cells that no inner strip covers (rows 1..nz-nbd, columns
+    // nbd+1..nx-nbd) at u^{n+1}, from the plane the step has just written: the reference forms the
+    // absorbing layers' operator field after its interior update.
     {
         const float* const uxq = a.top_pass ? a.ux[a.cur ^ 1] : uxc;
         const float* const uzq = a.top_pass ? a.uz[a.cur ^ 1] : uzc;
         const int qz1 = nz - a.nbd, qx0 = a.nbd + 1, qx1 = nx - a.nbd;
-        constexpr int kFill = 2;
+        constexpr int kU = 3, kM = 2, kB = 2;
         const int P2 = T.UZ / 2, NP = P2 * T.UX;
-        Walk wu(tid, P2, kThreads);   // (pair row, column) of this thread's items, in order
-        for (int i0 = tid; i0 < NP; i0 += kFill * kThreads) {
-            float2 vx[kFill], vz[kFill];
+        const int M2 = T.MZ / 2, NMP = M2 * T.MX;
+        // the strip rectangles met by the field tile: element e of their concatenation is row
+        // e % nzr_k, column e / nzr_k of rectangle k
+        const int zt0 = R.z0 - OU, zt1 = R.z0 - OU + T.UZ - 1;
+        const int xt0 = R.x0 - H, xt1 = R.x0 - H + T.UX - 1;
+        int bz0[3], bx0[3], bnz[3], bcnt[3];
+        const float* bxs[3];
+        const float* bzs[3];
+        long long brows[3], borg[3];
 #pragma unroll
-            for (int q = 0; q < kFill; ++q) {
-                const int i = i0 + q * kThreads;
+        for (int k = 0; k < 3; ++k) {
+            const StripRect S = strip_rect(a, pml, k);
+            const int z0 = max(max(S.zr0, 1), zt0), z1 = min(S.zr1, zt1);
+            // the right strips start after the left ones where the two would meet (narrow grids)
+            const int x0 = max(k == 1 && pml ? max(S.xr0, a.nbd + 1) : S.xr0, xt0), x1 = min(S.xr1, xt1);
+            const bool any = z0 <= z1 && x0 <= x1;
+            bz0[k] = z0; bx0[k] = x0;
+            bnz[k] = any ? z1 - z0 + 1 : 1;
+            bcnt[k] = any ? (z1 - z0 + 1) * (x1 - x0 + 1) : 0;
+            const long long plane = (long long)S.rows * S.cols * a.it;
+            bxs[k] = a.strip[S.sx] + plane;
+            bzs[k] = a.strip[S.sz] + plane;
+            brows[k] = S.rows;
+            borg[k] = (long long)S.zr0 + (long long)S.rows * S.xr0;   // strip offset = iz + rows ix - org
+        }
+        const int nb = bcnt[0] + bcnt[1] + bcnt[2];
+        // strip element e: its shared-memory offset in the field tile and its two values
+        auto bg_elem = [&](int e, int& off, float& vx, float& vz) {
+            int k = 0;
+            if (e >= bcnt[0]) { e -= bcnt[0]; k = 1; if (e >= bcnt[1]) { e -= bcnt[1]; k = 2; } }
+            int xq, zr;
+            divmod_small(e, k == 0 ? bnz[0] : k == 1 ? bnz[1] : bnz[2], xq, zr);
+            const int iz = (k == 0 ? bz0[0] : k == 1 ? bz0[1] : bz0[2]) + zr;
+            const int ix = (k == 0 ? bx0[0] : k == 1 ? bx0[1] : bx0[2]) + xq;
+            const long long o = (long long)iz + (k == 0 ? brows[0] : k == 1 ? brows[1] : brows[2]) * ix -
+                                (k == 0 ? borg[0] : k == 1 ? borg[1] : borg[2]);
+            vx = __ldg((k == 0 ? bxs[0] : k == 1 ? bxs[1] : bxs[2]) + o);
+            vz = __ldg((k == 0 ? bzs[0] : k == 1 ? bzs[1] : bzs[2]) + o);
+            off = (int)(SU(sux, iz - R.z0, ix - R.x0) - sux);
+        };
+        // the first kB strip elements of every thread, issued ahead of the field and material
+        // loads (every thread sets its offsets, so none is left undefined for the pass below)
+        float bvx[kB], bvz[kB];
+        int boff[kB];
+#pragma unroll
+        for (int q = 0; q < kB; ++q) {
+            boff[q] = -1;
+            bvx[q] = 0.f;
+            bvz[q] = 0.f;
+            const int e = tid + q * kThreads;
+            if (e < nb) bg_elem(e, boff[q], bvx[q], bvz[q]);
+        }
+        Walk wu(tid, P2, kThreads);   // (pair row, column) of this thread's field items, in order
+        Walk wm(tid, M2, kThreads);   // the same for the material items
+        for (int u0 = tid, m0 = tid; u0 < NP || m0 < NMP; u0 += kU * kThreads, m0 += kM * kThreads) {
+            float2 vx[kU], vz[kU], l[kM], m[kM];
+#pragma unroll
+            for (int q = 0; q < kU; ++q) {
+                const int i = u0 + q * kThreads;
                 const int iz = R.z0 - OU + 2 * wu.r, ix = R.x0 - H + wu.q;
                 wu.next();
                 vx[q] = f2s(0.f);
@@ -427,22 +484,8 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                 }
             }
 #pragma unroll
-            for (int q = 0; q < kFill; ++q) {
-                const int i = i0 + q * kThreads;
-                if (i < NP) {
-                    sts2(sux + 2 * i, vx[q]);
-                    sts2(suz + 2 * i, vz[q]);
-                }
-            }
-        }
-        constexpr int kFillM = 2;
-        const int M2 = T.MZ / 2, NMP = M2 * T.MX;
-        Walk wm(tid, M2, kThreads);
-        for (int i0 = tid; i0 < NMP; i0 += kFillM * kThreads) {
-            float2 l[kFillM], m[kFillM];
-#pragma unroll
-            for (int q = 0; q < kFillM; ++q) {
-                const int i = i0 + q * kThreads;
+            for (int q = 0; q < kM; ++q) {
+                const int i = m0 + q * kThreads;
                 const int iz = R.z0 - OM + 2 * wm.r, ix = R.x0 - NO + wm.q;
                 wm.next();
                 l[q] = f2s(0.f); m[q] = f2s(1.f);
@@ -453,8 +496,16 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                 }
             }
 #pragma unroll
-            for (int q = 0; q < kFillM; ++q) {
-                const int i = i0 + q * kThreads;
+            for (int q = 0; q < kU; ++q) {
+                const int i = u0 + q * kThreads;
+                if (i < NP) {
+                    sts2(sux + 2 * i, vx[q]);
+                    sts2(suz + 2 * i, vz[q]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kM; ++q) {
+                const int i = m0 + q * kThreads;
                 if (i < NMP) {
                     const float2 l2 = pfma(f2s(2.0f), m[q], l[q]);   // lambda + 2 mu (2 mu exact)
                     sts2(sLam + 2 * i, l[q]);
@@ -464,35 +515,19 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                 }
             }
         }
-    }
-    __syncthreads();
-    // the background strips that meet the u tile, added (regular field) or removed (absorbing
-    // layers' operator field) in place: one rounding per value, as u + b / u - b
-    {
-        const int zt0 = R.z0 - OU, zt1 = R.z0 - OU + T.UZ - 1;
-        const int xt0 = R.x0 - H, xt1 = R.x0 - H + T.UX - 1;
-#pragma unroll 1
-        for (int k = 0; k < 3; ++k) {
-            const StripRect S = strip_rect(a, pml, k);
-            const int z0 = max(max(S.zr0, 1), zt0), z1 = min(S.zr1, zt1);
-            // the right strips start after the left ones where the two would meet (narrow grids)
-            const int x0 = max(k == 1 && pml ? max(S.xr0, a.nbd + 1) : S.xr0, xt0), x1 = min(S.xr1, xt1);
-            if (z0 > z1 || x0 > x1) continue;
-            const int nzr = z1 - z0 + 1, n = nzr * (x1 - x0 + 1);
-            const long long plane = (long long)S.rows * S.cols * a.it;
-            const float* bxs = a.strip[S.sx] + plane;
-            const float* bzs = a.strip[S.sz] + plane;
-            for (int e = tid; e < n; e += kThreads) {
-                int xq, zr;
-                divmod_small(e, nzr, xq, zr);
-                const int iz = z0 + zr, ix = x0 + xq;
-                const long long o = (long long)(iz - S.zr0) + (long long)S.rows * (ix - S.xr0);
-                float* px = SU(sux, iz - R.z0, ix - R.x0);
-                float* pz = SU(suz, iz - R.z0, ix - R.x0);
-                const float bx = __ldg(bxs + o), bz = __ldg(bzs + o);
-                *px = pml ? __fsub_rn(*px, bx) : __fadd_rn(*px, bx);
-                *pz = pml ? __fsub_rn(*pz, bz) : __fadd_rn(*pz, bz);
-            }
+        __syncthreads();
+        auto bg_apply = [&](int off, float vxb, float vzb) {
+            sux[off] = pml ? __fsub_rn(sux[off], vxb) : __fadd_rn(sux[off], vxb);
+            suz[off] = pml ? __fsub_rn(suz[off], vzb) : __fadd_rn(suz[off], vzb);
+        };
+#pragma unroll
+        for (int q = 0; q < kB; ++q)
+            if (boff[q] >= 0) bg_apply(boff[q], bvx[q], bvz[q]);
+        for (int e = tid + kB * kThreads; e < nb; e += kThreads) {   // tiles with more strip cells
+            int off;
+            float vxb, vzb;
+            bg_elem(e, off, vxb, vzb);
+            bg_apply(off, vxb, vzb);
         }
     }
     __syncthreads();
