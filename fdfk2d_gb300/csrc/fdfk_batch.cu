@@ -1,6 +1,7 @@
 // Batches: many solves (sessions of one stencil order, any grid sizes) advanced
-// together.  Every step of the batch is three launches whatever the number of
-// members: a one-thread-per-member bump kernel that writes each member's time
+// together.  Every step of the batch is the same few launches whatever the number
+// of members (plus one for the top layers when a member has the absorbing layer
+// on top): a one-thread-per-member bump kernel that writes each member's time
 // index, plane parity and receiver sampling into its device-resident
 // StepArgs, then the fast path and the tiled kernel over all members' blocks
 // (two streams, as for one session).  The per-step kernels read everything
@@ -36,7 +37,8 @@ struct fdfk_batch {
     int* d_edge_off = nullptr;
     int* d_march_off = nullptr;
     int* d_frame_off = nullptr;
-    int edge_blocks = 0, march_blocks = 0, frame_blocks = 0;
+    int* d_top_off = nullptr;
+    int edge_blocks = 0, march_blocks = 0, frame_blocks = 0, top_blocks = 0;
     size_t smem = 0;
     bool dirty = true;         // tables do not match the members
     bool in_flight = false;    // device state newer than the members' host state
@@ -63,9 +65,9 @@ void drop_graph(fdfk_batch* b)
 void free_tables(fdfk_batch* b)
 {
     cudaFree(b->d_args); cudaFree(b->d_march); cudaFree(b->d_dyn); cudaFree(b->d_live);
-    cudaFree(b->d_edge_off); cudaFree(b->d_march_off); cudaFree(b->d_frame_off);
+    cudaFree(b->d_edge_off); cudaFree(b->d_march_off); cudaFree(b->d_frame_off); cudaFree(b->d_top_off);
     b->d_args = nullptr; b->d_march = nullptr; b->d_dyn = nullptr; b->d_live = nullptr;
-    b->d_edge_off = nullptr; b->d_march_off = nullptr; b->d_frame_off = nullptr;
+    b->d_edge_off = nullptr; b->d_march_off = nullptr; b->d_frame_off = nullptr; b->d_top_off = nullptr;
     b->cap = 0;
 }
 
@@ -80,6 +82,7 @@ BatchTab table(const fdfk_batch* b)
     t.edge_off = b->d_edge_off;
     t.march_off = b->d_march_off;
     t.frame_off = b->d_frame_off;
+    t.top_off = b->d_top_off;
     return t;
 }
 
@@ -118,6 +121,7 @@ int rebuild(fdfk_batch* b)
         if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_edge_off, (cap + 1) * sizeof(int));
         if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_march_off, (cap + 1) * sizeof(int));
         if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_frame_off, (cap + 1) * sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc((void**)&b->d_top_off, (cap + 1) * sizeof(int));
         if (e != cudaSuccess) {
             free_tables(b);
             return set_error(FDFK_ENOMEM, std::string("batch tables: ") + cudaGetErrorString(e));
@@ -127,7 +131,7 @@ int rebuild(fdfk_batch* b)
     std::vector<StepArgs> args(n);
     std::vector<MarchArgs> march(n);
     std::vector<BatchDyn> dyn(n);
-    std::vector<int> live(n, 0), eoff(n + 1, 0), moff(n + 1, 0), foff(n + 1, 0);
+    std::vector<int> live(n, 0), eoff(n + 1, 0), moff(n + 1, 0), foff(n + 1, 0), toff(n + 1, 0);
     size_t smem = 0;
     // fast-path segments re-planned for the whole batch: about two waves of resident warps over
     // all members' work, 16..48 columns per segment (a member alone plans for itself only)
@@ -169,6 +173,7 @@ int rebuild(fdfk_batch* b)
         eoff[i + 1] = eoff[i] + a.n_tiles + nsb;
         moff[i + 1] = moff[i] + (m.n_bands * m.n_segs + 3) / 4;
         foff[i + 1] = foff[i] + (m.n_bands > 0 ? frame_blocks(a) : 0);
+        toff[i + 1] = toff[i] + (a.izt != 1 ? a.tiles_t_z * a.tiles_t_x : 0);
         smem = std::max(smem, step_smem_for(a));
     }
     if (n) {
@@ -179,15 +184,18 @@ int rebuild(fdfk_batch* b)
         BK(cudaMemcpy(b->d_edge_off, eoff.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
         BK(cudaMemcpy(b->d_march_off, moff.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
         BK(cudaMemcpy(b->d_frame_off, foff.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        BK(cudaMemcpy(b->d_top_off, toff.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
     }
     b->edge_blocks = eoff[n];
     b->march_blocks = moff[n];
     b->frame_blocks = foff[n];
+    b->top_blocks = toff[n];
     b->smem = smem;
     // opt the batched kernels into their shared memory outside any stream capture
     const BatchTab t = table(b);
     if (n) {
         BK(launch_step_batch(t, b->norder, 0, b->smem, b->stream));
+        BK(launch_step_top_batch(t, b->norder, 0, b->smem, b->stream));
         if (b->norder <= kMarchMaxOrder) BK(launch_march_batch(t, b->norder, 0, 0, b->stream));
     }
     b->dirty = false;
@@ -208,10 +216,13 @@ cudaError_t step_once(fdfk_batch* b)
         (e = launch_march_batch(t, b->norder, b->frame_blocks, b->march_blocks, b->stream)) != cudaSuccess)
         return e;
     if ((e = cudaEventRecord(b->join, b->side)) != cudaSuccess) return e;
-    return cudaStreamWaitEvent(b->stream, b->join, 0);
+    if ((e = cudaStreamWaitEvent(b->stream, b->join, 0)) != cudaSuccess) return e;
+    // members with the absorbing layer on top: their top layers read the interior just updated
+    if (b->top_blocks > 0) return launch_step_top_batch(t, b->norder, b->top_blocks, b->smem, b->stream);
+    return cudaSuccess;
 }
 
-int launches_per_step(const fdfk_batch* b) { return 2 + (b->march_blocks > 0 ? 2 : 0); }
+int launches_per_step(const fdfk_batch* b) { return 2 + (b->march_blocks > 0 ? 2 : 0) + (b->top_blocks > 0 ? 1 : 0); }
 
 }  // namespace
 
@@ -245,9 +256,6 @@ int fdfk_batch_add(fdfk_batch* b, fdfk_session* s)
     if (!b || !s) return set_error(FDFK_EINVAL, "NULL argument");
     if (s->batch) return set_error(FDFK_ESTATE, "the session already belongs to a batch");
     if (s->p.norder != b->norder) return set_error(FDFK_EINVAL, "the session's norder differs from the batch's");
-    if (s->izt != 1)
-        return set_error(FDFK_EUNSUPPORTED, "a session with the absorbing layer on top steps alone (its top layer "
-                                            "needs a launch after the interior update)");
     for (int t = s->it; t <= s->p.nt; ++t)
         if (!s->have_bg[t]) return set_error(FDFK_ESTATE, "the session has no background for time index " + std::to_string(t));
     int rc = pull(b);

@@ -135,7 +135,6 @@ int fdfk_server_submit(fdfk_server* sv, const fdfk_solve_request* r, long long* 
 {
     if (!sv || !r || !id) return set_error(FDFK_EINVAL, "NULL argument");
     if (r->p.norder != sv->norder) return set_error(FDFK_EINVAL, "the request's norder differs from the server's");
-    if (r->p.is_PML_top) return set_error(FDFK_EUNSUPPORTED, "requests with the absorbing layer on top are solved alone");
     if (!r->c || !r->bazs || !r->fk_left || !r->fk_right || !r->seisx || !r->seisz || r->nrcv < 1 || r->nsis < 0)
         return set_error(FDFK_EINVAL, "request: missing inputs or outputs");
     Req* q = new (std::nothrow) Req();

@@ -1010,6 +1010,24 @@ __global__ void __launch_bounds__(kThreads, 3) fdfk_step_batch_kernel(BatchTab t
     step_block<NO>(sa, blockIdx.x - t.edge_off[s]);
 }
 
+// The top layers of the members with the absorbing layer on top: member s owns blocks
+// top_off[s] .. top_off[s+1]-1 of this launch, queued after the step's interior update.
+template <int NO>
+__global__ void __launch_bounds__(kThreads, 3) fdfk_step_top_batch_kernel(BatchTab t)
+{
+    __shared__ StepArgs sa;
+    const int s = batch_member(t.top_off, t.n, blockIdx.x);
+    if (!t.live[s]) return;                // the whole block returns: no barrier is split
+    stage_args(sa, t.args + s);
+    if (threadIdx.x == 0) {
+        sa.top_pass = 1;
+        sa.n_tiles = sa.tiles_t_z * sa.tiles_t_x;
+        sa.nrcv = 0;
+    }
+    __syncthreads();
+    step_block<NO>(sa, blockIdx.x - t.top_off[s]);
+}
+
 // Per-step bookkeeping of a batch on the device: time index, plane parity and receiver sampling of
 // every member, written into its StepArgs before the step's kernels run.
 __global__ void fdfk_batch_bump(BatchTab t)
@@ -1123,6 +1141,36 @@ cudaError_t launch_step_batch(const BatchTab& t, int norder, int blocks, size_t 
     case 6: return launch_batch_no<6>(t, blocks, smem, s);
     case 7: return launch_batch_no<7>(t, blocks, smem, s);
     case 8: return launch_batch_no<8>(t, blocks, smem, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int NO>
+static cudaError_t launch_top_batch_no(const BatchTab& t, int blocks, size_t smem, cudaStream_t s)
+{
+    static int configured = 0;
+    if ((int)smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(fdfk_step_top_batch_kernel<NO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = (int)smem;
+    }
+    if (blocks == 0) return cudaSuccess;
+    fdfk_step_top_batch_kernel<NO><<<blocks, kThreads, smem, s>>>(t);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step_top_batch(const BatchTab& t, int norder, int blocks, size_t smem, cudaStream_t s)
+{
+    switch (norder) {
+    case 1: return launch_top_batch_no<1>(t, blocks, smem, s);
+    case 2: return launch_top_batch_no<2>(t, blocks, smem, s);
+    case 3: return launch_top_batch_no<3>(t, blocks, smem, s);
+    case 4: return launch_top_batch_no<4>(t, blocks, smem, s);
+    case 5: return launch_top_batch_no<5>(t, blocks, smem, s);
+    case 6: return launch_top_batch_no<6>(t, blocks, smem, s);
+    case 7: return launch_top_batch_no<7>(t, blocks, smem, s);
+    case 8: return launch_top_batch_no<8>(t, blocks, smem, s);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -130,12 +130,15 @@ struct BatchTab {
     const int* edge_off;      // [n+1] first tiled-kernel block of each member
     const int* march_off;     // [n+1] first fast-path block of each member
     const int* frame_off;     // [n+1] first frame block of each member
+    const int* top_off;       // [n+1] first block of each member's top-layer launch (izt < 1)
 };
 
 cudaError_t launch_step_batch(const BatchTab& t, int norder, int blocks, size_t smem, cudaStream_t s);
 // The top absorbing layer's launch of one solve (izt < 1): after the interior update of the step,
 // whose new values the layer's operator field reads (a with top_pass set by the call).
 cudaError_t launch_step_top(const StepArgs& a, cudaStream_t s);
+// The top layers of a batch's members with the absorbing layer on top, after the step's interior.
+cudaError_t launch_step_top_batch(const BatchTab& t, int norder, int blocks, size_t smem, cudaStream_t s);
 cudaError_t launch_batch_bump(const BatchTab& t, cudaStream_t s);
 // Frame (frame_blocks blocks) and fast path (blocks blocks) of a batch step.
 cudaError_t launch_march_batch(const BatchTab& t, int norder, int frame_blocks, int blocks, cudaStream_t s);

@@ -5,8 +5,8 @@
 * Whole time loops through the C ABI against the oracle's restatement of the mode
   (oracle/fdfk_oracle.c, item 5), receivers on the surface (whose 7 x 7 sampling reaches into
   the top layer) and below it.
-* The fast path and the all-tiled path agree, every launch shape gives the same bits, and a batch
-  refuses the mode (its top layer needs a launch after the interior update).
+* The fast path and the all-tiled path agree, every launch shape gives the same bits, and batched
+  members (their top layers in one more launch after the step's interior) match their solves alone.
 """
 import os
 
@@ -112,10 +112,29 @@ def test_fast_path_tiled_path_and_tunings_agree(F):
         assert np.array_equal(other[0], fast[0]) and np.array_equal(other[1], fast[1]), tune
 
 
-def test_batch_refuses_top_sessions(F):
-    p, c, strips, rx, rz = _top_case(5, 40, 24, 6, 2, 20)
-    with F.Session(p, c) as s, F.Batch(2) as b:
+def test_batch_with_top_sessions_matches_each_alone(F):
+    """Members with the absorbing layer on top (and one with a free surface) in one batch, with
+    graph replay: every member's seismograms are the bits it gets alone."""
+    cases = [_top_case(61, 70, 37, 10, 3, 140), _top_case(62, 55, 30, 9, 3, 100)]
+    free = _top_case(63, 60, 33, 8, 3, 120)
+    p_free = dict(free[0], is_PML_top=False)
+    c_free = np.asfortranarray(free[1][:, free[0]["npml"]:, :])
+    cases.append((p_free, c_free, free[2], free[3], free[4]))
+    ref = [_solve(F, *cs) for cs in cases]
+    sessions = []
+    for p, c, strips, rx, rz in cases:
+        s = F.Session(p, c)
         s.upload_background(strips)
-        with pytest.raises(F.FDFKError) as e:
+        s.set_receivers(rx, rz, 0.0, 0.0, 1, p["nt"])
+        sessions.append(s)
+    with F.Batch(3, graph_chunk=16) as b:
+        for s in sessions:
             b.add(s)
-        assert e.value.code == -2
+        b.advance(141)
+        assert b.live() == 0
+        got = [s.seismograms() for s in sessions]
+    for (gx, gz), (rx_, rz_) in zip(got, ref):
+        assert np.abs(gz).max() > 0
+        assert np.array_equal(gx, rx_) and np.array_equal(gz, rz_)
+    for s in sessions:
+        s.close()
