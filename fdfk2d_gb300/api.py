@@ -114,6 +114,7 @@ def lib():
                      "fdfk_session_download_seismogram_range", "fdfk_session_advance_timed",
                      "fdfk_session_interior_cells", "fdfk_session_fk_background", "fdfk_fk_background",
                      "fdfk_batch_create", "fdfk_batch_add", "fdfk_batch_remove", "fdfk_batch_set_graph_chunk",
+                     "fdfk_batch_set_tuning",
                      "fdfk_batch_advance", "fdfk_batch_synchronize", "fdfk_batch_live", "fdfk_batch_size",
                      "fdfk_server_create", "fdfk_server_submit", "fdfk_server_pump", "fdfk_server_request",
                      "fdfk_server_get_stats", "fdfk_input_read", "fdfk_backazimuths", "fdfk_stable_dt",
@@ -301,6 +302,11 @@ class Batch:
     def add(self, session: "Session"):
         _check(lib().fdfk_batch_add(self._h, session._h))
         self.members.append(session)
+
+    def set_tuning(self, seg_len: int = 0, pml_run: int = 0):
+        """Launch shapes for every member while batched (0: planned for the batch / each member's
+        own); the results do not depend on them."""
+        _check(lib().fdfk_batch_set_tuning(self._h, C.c_int(int(seg_len)), C.c_int(int(pml_run))))
 
     def remove(self, session: "Session"):
         _check(lib().fdfk_batch_remove(self._h, session._h))

@@ -43,6 +43,8 @@ struct fdfk_batch {
     bool dirty = true;         // tables do not match the members
     bool in_flight = false;    // device state newer than the members' host state
     int chunk = 32;            // steps per captured graph (0: no graph)
+    int seg_len = 0;           // fast-path segment columns for every member (0: planned for the batch)
+    int pml_run = 0;           // absorbing-layer tile length for every member (0: each member's own)
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
 };
@@ -143,9 +145,15 @@ int rebuild(fdfk_batch* b)
         seg = (int)((work + 2LL * slots - 1) / (2LL * slots));
         seg = seg < 16 ? 16 : seg > 48 ? 48 : seg;
     }
+    if (b->seg_len > 0) seg = b->seg_len;
     for (int i = 0; i < n; ++i) {
         const fdfk_session* s = b->members[i];
         StepArgs a = s->base;
+        if (b->pml_run > 0) {   // the batch's absorbing-layer tiles, where they fit a block
+            StepArgs t = a;
+            plan_tiles(t, s->march.n_bands > 0, b->pml_run);
+            if (step_smem_for(t) <= (size_t)227 * 1024) a = t;
+        }
         for (int l = 0; l < 2; ++l) { a.ux[l] = s->ux[l]; a.uz[l] = s->uz[l]; }
         for (int q = 0; q < 24; ++q) for (int l = 0; l < 2; ++l) a.bu[q][l] = s->bu[q][l];
         for (int q = 0; q < 12; ++q) a.bp[q] = s->bp[q];
@@ -281,6 +289,18 @@ int fdfk_batch_remove(fdfk_batch* b, fdfk_session* s)
     if (rc) return rc;
     b->members.erase(std::find(b->members.begin(), b->members.end(), s));
     s->batch = nullptr;
+    b->dirty = true;
+    return FDFK_OK;
+}
+
+int fdfk_batch_set_tuning(fdfk_batch* b, int seg_len, int pml_run)
+{
+    if (!b || (seg_len != 0 && (seg_len < 8 || seg_len > 1024)) || (pml_run != 0 && (pml_run < 8 || pml_run > 64)))
+        return set_error(FDFK_EINVAL, "segment length must be 8..1024 and tile length 8..64 (0: the default)");
+    int rc = pull(b);
+    if (rc) return rc;
+    b->seg_len = seg_len;
+    b->pml_run = pml_run;
     b->dirty = true;
     return FDFK_OK;
 }

@@ -40,7 +40,7 @@ typedef struct fdfk_params {
     int nx, nz;     /* interior grid */
     int npml;       /* absorbing-layer width in cells (>= 2*norder-1) */
     int is_PML_top; /* reference logical: 0 free surface on top (izt = 1), 1 absorbing layer on top
-                       (izt = 1 - npml: npml more rows above row 1; sessions step alone, not in batches) */
+                       (izt = 1 - npml: npml more rows above row 1) */
     int npower;     /* damping profile exponent (reference: 2) */
     int nbd;        /* background-strip width, 2*norder-1 */
     int nt;         /* last time index; strips hold nt+1 samples */
@@ -257,6 +257,10 @@ int fdfk_batch_add(fdfk_batch* b, fdfk_session* s);
 int fdfk_batch_remove(fdfk_batch* b, fdfk_session* s);
 /* Steps per captured graph (default 32; 0 launches step by step). */
 int fdfk_batch_set_graph_chunk(fdfk_batch* b, int steps);
+/* Launch shapes for every member while in this batch: fast-path segment columns (8..1024; 0 plans
+ * them for the batch, about two waves of resident warps) and absorbing-layer tile length (8..64;
+ * 0 keeps each member's own).  Results do not depend on either. */
+int fdfk_batch_set_tuning(fdfk_batch* b, int seg_len, int pml_run);
 /* Advance every member by nsteps (a member past its nt does nothing). Asynchronous. */
 int fdfk_batch_advance(fdfk_batch* b, int nsteps);
 /* Wait for the batch and bring the members' step counters up to date. */

@@ -164,3 +164,29 @@ def test_batch_matches_shipped_loop(F):
     err = np.linalg.norm(sz - d["seisz"]) / np.linalg.norm(d["seisz"])
     assert err < 1e-4
     assert np.array_equal(sx, tx) and np.array_equal(sz, tz)
+
+
+@pytest.mark.parametrize("seg,run", [(24, 16), (0, 13), (64, 0)])
+def test_batch_tuning_changes_no_result(F, seg, run):
+    """The batch's own launch shapes (segment columns, absorbing-layer tile length) give every
+    member the bits it gets alone."""
+    ref = [_alone(F, e) for e in EVENTS[:3]]
+    sessions = [_session(F, *e) for e in EVENTS[:3]]
+    with F.Batch(3, graph_chunk=16) as b:
+        b.set_tuning(seg, run)
+        for s in sessions:
+            b.add(s)
+        b.advance(120)
+        b.set_tuning(0, 0)                 # back to the defaults half-way
+        b.advance(121)
+        got = [s.seismograms() for s in sessions]
+    for (gx, gz), (rx_, rz_) in zip(got, ref):
+        assert np.array_equal(gx, rx_) and np.array_equal(gz, rz_)
+    with pytest.raises(F.FDFKError):
+        b2 = F.Batch(3)
+        try:
+            b2.set_tuning(4, 0)
+        finally:
+            b2.close()
+    for s in sessions:
+        s.close()
