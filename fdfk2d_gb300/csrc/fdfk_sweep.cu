@@ -58,7 +58,7 @@ __host__ __device__ __forceinline__ TileDims tile_dims(int NO, int TZ, int TX)
     t.U = t.UZ * t.UX; t.M = t.MZ * t.MX;
     t.AX = t.TZe * t.XW; t.AZ = t.ZW * TX;
     t.FS = kFsTerms * TX;
-    t.total = 2 * t.U + 4 * t.M + 4 * t.AX + 4 * t.AZ + ((t.FS + 1) & ~1);
+    t.total = 2 * t.U + 4 * t.M + 6 * t.AX + 6 * t.AZ + ((t.FS + 1) & ~1);
     return t;
 }
 
@@ -370,13 +370,21 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
     float* sMu = sLam + T.M;
     float* sRL2m = sMu + T.M;
     float* sRMu = sRL2m + T.M;
+    // The staggered products at a half point L enter the second derivatives of the cells on both
+    // sides of it: with the stencil order of column (row) L for the cells at or before L (gxA,
+    // gxB, gzA, gzB) and with the order of column (row) L+1 for the cells after it (the "m"
+    // arrays).  The two differ only next to the outer frame and the top rows, where the order drops.
     float* gxA = sRMu + T.M;   // H(l2m) * Dstag_x(ux)   [label][z]
     float* gxB = gxA + T.AX;   // H(mu)  * Dstag_x(uz)
-    float* v1 = gxB + T.AX;    // lam * Dz(uz)/dz        [x][z]  (dzx(lam uz))
+    float* gxAm = gxB + T.AX;  // the same with the order of column L+1
+    float* gxBm = gxAm + T.AX;
+    float* v1 = gxBm + T.AX;   // lam * Dz(uz)/dz        [x][z]  (dzx(lam uz))
     float* v4 = v1 + T.AX;     // mu  * Dz(ux)/dz                 (dzx(mu ux))
     float* gzA = v4 + T.AX;    // H(l2m) * Dstag_z(uz)   [x][label]
     float* gzB = gzA + T.AZ;   // H(mu)  * Dstag_z(ux)
-    float* v2 = gzB + T.AZ;    // mu  * Dx(uz)/dx        [x][z]  (dxz(mu uz))
+    float* gzAm = gzB + T.AZ;  // the same with the order of row L+1
+    float* gzBm = gzAm + T.AZ;
+    float* v2 = gzBm + T.AZ;   // mu  * Dx(uz)/dx        [x][z]  (dxz(mu uz))
     float* v3 = v2 + T.AZ;     // lam * Dx(ux)/dx                 (dxz(lam ux))
     float* sFS = v3 + T.AZ;    // free-surface terms of row 1       [term][x]
 
@@ -591,7 +599,7 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             // staggered products at label L = xl - NO (half point between columns L and L+1)
             if (xl < T.XW - 1) {
                 const int L = xl - NO;
-                const int n = ordx(a, R.x0 + L, NO);
+                const int n = ordx(a, R.x0 + L, NO), nm = ordx(a, R.x0 + L + 1, NO);
                 float2 sx = f2s(0.f), szv = f2s(0.f);
 #pragma unroll
                 for (int j = 1; j <= NO; ++j) {
@@ -601,8 +609,23 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                 }
                 const float2 rl = padd(lds2(SM(sRL2m, z, L)), lds2(SM(sRL2m, z, L + 1)));
                 const float2 rm = padd(lds2(SM(sRMu, z, L)), lds2(SM(sRMu, z, L + 1)));
-                sts2(gxA + o, pmul(f2(2.0f * fast_rcp(rl.x), 2.0f * fast_rcp(rl.y)), sx));
-                sts2(gxB + o, pmul(f2(2.0f * fast_rcp(rm.x), 2.0f * fast_rcp(rm.y)), szv));
+                const float2 hl = f2(2.0f * fast_rcp(rl.x), 2.0f * fast_rcp(rl.y));
+                const float2 hm = f2(2.0f * fast_rcp(rm.x), 2.0f * fast_rcp(rm.y));
+                sts2(gxA + o, pmul(hl, sx));
+                sts2(gxB + o, pmul(hm, szv));
+                float2 sxm = sx, szm = szv;
+                if (nm != n) {
+                    sxm = f2s(0.f);
+                    szm = f2s(0.f);
+#pragma unroll
+                    for (int j = 1; j <= NO; ++j) {
+                        const float2 c = f2s(c_stag[nm][j]);
+                        sxm = pfma(c, psub(lds2(SU(sux, z, L + j)), lds2(SU(sux, z, L + 1 - j))), sxm);
+                        szm = pfma(c, psub(lds2(SU(suz, z, L + j)), lds2(SU(suz, z, L + 1 - j))), szm);
+                    }
+                }
+                sts2(gxAm + o, pmul(hl, sxm));
+                sts2(gxBm + o, pmul(hm, szm));
             }
             // dzx operands at column x = xl - NO
             {
@@ -641,7 +664,7 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             const int ix = R.x0 + x;
             const int o = x * T.ZW + (L + OM);
             if (L <= TZ + NO - 2) {   // labels read by the output cells: -NO .. TZ+NO-2
-                const int n0 = ordz(a, R.z0 + L, NO), n1 = ordz(a, R.z0 + L + 1, NO);
+                const int n0 = ordz(a, R.z0 + L, NO), n1 = ordz(a, R.z0 + L + 1, NO), n2 = ordz(a, R.z0 + L + 2, NO);
                 // rows L+1-NO .. L+1+NO from the even row L - B
                 constexpr int B = 2 * (NO / 2);
                 float wz[NO + B + 2], wx[NO + B + 2];
@@ -655,6 +678,18 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                     szv = pfma(c, f2(__fsub_rn(wz[B + j], wz[B + 1 - j]), __fsub_rn(wz[B + 1 + j], wz[B + 2 - j])), szv);
                     sx = pfma(c, f2(__fsub_rn(wx[B + j], wx[B + 1 - j]), __fsub_rn(wx[B + 1 + j], wx[B + 2 - j])), sx);
                 }
+                // the same half points with the orders of rows L+1 and L+2
+                float2 szm = szv, sxm = sx;
+                if (n0 != n1 || n1 != n2) {
+                    szm = f2s(0.f);
+                    sxm = f2s(0.f);
+#pragma unroll
+                    for (int j = 1; j <= NO; ++j) {
+                        const float2 c = f2(c_stag[n1][j], c_stag[n2][j]);
+                        szm = pfma(c, f2(__fsub_rn(wz[B + j], wz[B + 1 - j]), __fsub_rn(wz[B + 1 + j], wz[B + 2 - j])), szm);
+                        sxm = pfma(c, f2(__fsub_rn(wx[B + j], wx[B + 1 - j]), __fsub_rn(wx[B + 1 + j], wx[B + 2 - j])), sxm);
+                    }
+                }
                 // harmonic means over rows (L, L+1) and (L+1, L+2); row L+2 only where half point
                 // L+1 is read (the material tile ends at row TZe+OM-1)
                 const int L2 = L + 1 <= TZ + NO - 2 ? L + 2 : L + 1;
@@ -664,6 +699,8 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                 const float2 hm = f2(2.0f * fast_rcp(__fadd_rn(rm.x, rm.y)), 2.0f * fast_rcp(__fadd_rn(rm.y, rm2)));
                 sts2(gzA + o, pmul(hl, szv));
                 sts2(gzB + o, pmul(hm, sx));
+                sts2(gzAm + o, pmul(hl, szm));
+                sts2(gzBm + o, pmul(hm, sxm));
             }
             // dxz operands at rows L, L+1
             {
@@ -726,74 +763,37 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
 
         const int nxo = ordx(a, ix, NO);
         const int nz0 = ordz(a, iz, NO), nz1 = ordz(a, iz + 1, NO);
-        // every column ix-NO..ix (row iz-NO..iz) has the full order: no reduced-order half points
-        const bool fullx = ix - NO >= NO - npml + 1 && ix <= nx + npml - NO;
-        const bool fullz0 = iz - NO >= NO + izt && iz <= NZ - NO;
-        const bool fullz1 = iz + 1 - NO >= NO + izt && iz + 1 <= NZ - NO;
         const float2 kd = f2(__ldg(a.kdt2 + g), __ldg(a.kdt2 + g1));
 
-        // x-direction second derivatives dxx(l2m ux), dxx(mu uz)
+        // x-direction second derivatives dxx(l2m ux), dxx(mu uz): half points x+k-1 after the cell,
+        // x-k before it (the latter with the order of the column after the half point)
         float2 x2a = f2s(0.f), x2b = f2s(0.f);
 #pragma unroll
         for (int k = 1; k <= NO; ++k) {
             const float2 c = f2s(c_stag[nxo][k]);
             const float2 pa = lds2(GX(gxA, z, x + k - 1)), pb = lds2(GX(gxB, z, x + k - 1));
-            float2 ma, mb;
-            const int Lm = x - k;
-            const int nr = fullx ? NO : ordx(a, ix - k + 1, NO);
-            if (fullx || nr == ordx(a, ix - k, NO)) {
-                ma = lds2(GX(gxA, z, Lm));
-                mb = lds2(GX(gxB, z, Lm));
-            } else {
-                float2 s1 = f2s(0.f), s2 = f2s(0.f);
-                for (int j = 1; j <= NO; ++j) {
-                    const float2 cj = f2s(c_stag[nr][j]);
-                    s1 = pfma(cj, psub(lds2(SU(sux, z, Lm + j)), lds2(SU(sux, z, Lm + 1 - j))), s1);
-                    s2 = pfma(cj, psub(lds2(SU(suz, z, Lm + j)), lds2(SU(suz, z, Lm + 1 - j))), s2);
-                }
-                const float2 rl = padd(lds2(SM(sRL2m, z, Lm)), lds2(SM(sRL2m, z, Lm + 1)));
-                const float2 rm = padd(lds2(SM(sRMu, z, Lm)), lds2(SM(sRMu, z, Lm + 1)));
-                ma = pmul(f2(__fdiv_rn(2.0f, rl.x), __fdiv_rn(2.0f, rl.y)), s1);
-                mb = pmul(f2(__fdiv_rn(2.0f, rm.x), __fdiv_rn(2.0f, rm.y)), s2);
-            }
+            const float2 ma = lds2(GX(gxAm, z, x - k)), mb = lds2(GX(gxBm, z, x - k));
             x2a = pfma(c, psub(pa, ma), x2a);
             x2b = pfma(c, psub(pb, mb), x2b);
         }
         const float2 Fx2_l2m_ux = pmul(x2a, dx2);
         const float2 Fx2_mu_uz = pmul(x2b, dx2);
 
-        // z-direction second derivatives dzz(l2m uz), dzz(mu ux); the products at the reduced-order
-        // half points next to the top rows and the outer frame are recomputed with the cell's order
+        // z-direction second derivatives dzz(l2m uz), dzz(mu ux): half points after the rows from
+        // gzA / gzB, before them from gzAm / gzBm
         float2 z2a = f2s(0.f), z2b = f2s(0.f);
         {
-            float ga[OM + NO + 1], gb[OM + NO + 1];   // labels z-OM .. z+NO
-            load_rows(GZ(gzA, z - OM, x), ga);
-            load_rows(GZ(gzB, z - OM, x), gb);
+            float pa[NO + 1], pb[NO + 1];   // labels z .. z+NO
+            float ma[OM + 1], mb[OM + 1];   // labels z-OM .. z
+            load_rows(GZ(gzA, z, x), pa);
+            load_rows(GZ(gzB, z, x), pb);
+            load_rows(GZ(gzAm, z - OM, x), ma);
+            load_rows(GZ(gzBm, z - OM, x), mb);
 #pragma unroll
             for (int k = 1; k <= NO; ++k) {
                 const float2 c = f2(c_stag[nz0][k], c_stag[nz1][k]);
-                float ma0 = ga[OM - k], ma1 = ga[OM + 1 - k], mb0 = gb[OM - k], mb1 = gb[OM + 1 - k];
-                if (!(fullz0 && fullz1)) {
-#pragma unroll
-                    for (int r = 0; r < 2; ++r) {
-                        const int izr = iz + r;
-                        const int nr = ordz(a, izr - k + 1, NO);
-                        if ((r == 0 ? fullz0 : fullz1) || nr == ordz(a, izr - k, NO)) continue;
-                        const int Lm = z + r - k;
-                        float s1 = 0.f, s2 = 0.f;
-                        for (int j = 1; j <= NO; ++j) {
-                            const float cj = c_stag[nr][j];
-                            s1 = fmaf(cj, __fsub_rn(*SU(suz, Lm + j, x), *SU(suz, Lm + 1 - j, x)), s1);
-                            s2 = fmaf(cj, __fsub_rn(*SU(sux, Lm + j, x), *SU(sux, Lm + 1 - j, x)), s2);
-                        }
-                        const float ra = __fmul_rn(__fdiv_rn(2.0f, __fadd_rn(*SM(sRL2m, Lm, x), *SM(sRL2m, Lm + 1, x))), s1);
-                        const float rb = __fmul_rn(__fdiv_rn(2.0f, __fadd_rn(*SM(sRMu, Lm, x), *SM(sRMu, Lm + 1, x))), s2);
-                        if (r == 0) { ma0 = ra; mb0 = rb; }
-                        else { ma1 = ra; mb1 = rb; }
-                    }
-                }
-                z2a = pfma(c, f2(__fsub_rn(ga[OM + k - 1], ma0), __fsub_rn(ga[OM + k], ma1)), z2a);
-                z2b = pfma(c, f2(__fsub_rn(gb[OM + k - 1], mb0), __fsub_rn(gb[OM + k], mb1)), z2b);
+                z2a = pfma(c, f2(__fsub_rn(pa[k - 1], ma[OM - k]), __fsub_rn(pa[k], ma[OM + 1 - k])), z2a);
+                z2b = pfma(c, f2(__fsub_rn(pb[k - 1], mb[OM - k]), __fsub_rn(pb[k], mb[OM + 1 - k])), z2b);
             }
         }
         const float2 Fz2_l2m_uz = pmul(z2a, dz2);
