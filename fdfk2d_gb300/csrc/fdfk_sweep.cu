@@ -93,14 +93,11 @@ __device__ __forceinline__ void divmod_small(int x, int n, int& q, int& r)
     }
 }
 
-// (i % n, i / n) along i = i0, i0 + step, ... without a division per step.
+// (i % n, i / n) along i = i0, i0 + step, ... without a division per step: from (i0 / n, i0 % n)
+// and (step / n, step % n).
 struct Walk {
     int r, q, dr, dq, n;
-    __device__ __forceinline__ Walk(int i0, int n_, int step) : n(n_)
-    {
-        divmod_small(i0, n_, q, r);
-        divmod_small(step, n_, dq, dr);
-    }
+    __device__ __forceinline__ Walk(int q0, int r0, int dq_, int dr_, int n_) : r(r0), q(q0), dr(dr_), dq(dq_), n(n_) {}
     __device__ __forceinline__ void next()
     {
         r += dr;
@@ -149,30 +146,6 @@ __device__ __forceinline__ const float* outer_bg_ptr(const StepArgs& a, int iz, 
         return a.strip[UXB_PML] + o;
     }
     return nullptr;
-}
-
-// One background strip as a rectangle of the grid: rows zr0..zr1, columns xr0..xr1, stored as
-// strip[(iz - zr0) + rows * ((ix - xr0) + cols * it)] (time slowest).  inner: the strips inside
-// the regular domain (Omega_I, removed from the absorbing layers' operator field), else the outer
-// strips (Omega_II, added to the regular field); k = 0 left, 1 right, 2 bottom.
-struct StripRect {
-    int zr0, zr1, xr0, xr1, rows, cols, sx, sz;
-};
-
-__device__ __forceinline__ StripRect strip_rect(const StepArgs& a, bool inner, int k)
-{
-    const int nx = a.nx, nz = a.nz, nbd = a.nbd;
-    StripRect r;
-    if (inner) {
-        if (k == 0) r = {1, nz - nbd, 1, nbd, nz - nbd, nbd, UXL_REG, UZL_REG};
-        else if (k == 1) r = {1, nz - nbd, nx - nbd + 1, nx, nz - nbd, nbd, UXR_REG, UZR_REG};
-        else r = {nz - nbd + 1, nz, 1, nx, nbd, nx, UXB_REG, UZB_REG};
-    } else {
-        if (k == 0) r = {1, nz, 1 - nbd, 0, nz, nbd, UXL_PML, UZL_PML};
-        else if (k == 1) r = {1, nz, nx + 1, nx + nbd, nz, nbd, UXR_PML, UZR_PML};
-        else r = {nz + 1, nz + nbd, 1 - nbd, nx + nbd, nbd, nx + 2 * nbd, UXB_PML, UZB_PML};
-    }
-    return r;
 }
 
 __device__ __forceinline__ Rect decode_tile(const StepArgs& a, int b)
@@ -394,6 +367,16 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
 #define GZ(arr, L, x) ((arr) + (x) * T.ZW + ((L) + OM))
 
     const float rdx = 1.0f / a.dx, rdz = 1.0f / a.dz;
+    // this thread's first item in the pair-row grids of P2 (field tile), M2 (material tile,
+    // z-direction products) and PZ (x-direction products, output cells) pair rows; the block's
+    // stride through them comes with the tile class
+    const int P2 = T.UZ / 2, M2 = T.MZ / 2, PZ = TZe / 2;
+    int qU, rU, qM, rM, qP, rP;
+    divmod_small(tid, P2, qU, rU);
+    divmod_small(tid, M2, qM, rM);
+    divmod_small(tid, PZ, qP, rP);
+    const int* const wq = a.wq[R.cls];
+    const int* const wr = a.wr[R.cls];
     const float* uxc = a.ux[a.cur];
     const float* uzc = a.uz[a.cur];
     const int izt = a.izt;
@@ -412,31 +395,28 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         const float* const uzq = a.top_pass ? a.uz[a.cur ^ 1] : uzc;
         const int qz1 = nz - a.nbd, qx0 = a.nbd + 1, qx1 = nx - a.nbd;
         constexpr int kU = 3, kM = 2, kB = 2;
-        const int P2 = T.UZ / 2, NP = P2 * T.UX;
-        const int M2 = T.MZ / 2, NMP = M2 * T.MX;
+        const int NP = P2 * T.UX, NMP = M2 * T.MX;
         // the strip rectangles met by the field tile: element e of their concatenation is row
         // e % nzr_k, column e / nzr_k of rectangle k
         const int zt0 = R.z0 - OU, zt1 = R.z0 - OU + T.UZ - 1;
         const int xt0 = R.x0 - H, xt1 = R.x0 - H + T.UX - 1;
-        int bz0[3], bx0[3], bnz[3], bcnt[3];
+        int bz0[3], bx0[3], bnz[3], bcnt[3], brows[3], borg[3];
         const float* bxs[3];
         const float* bzs[3];
-        long long brows[3], borg[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            const StripRect S = strip_rect(a, pml, k);
-            const int z0 = max(max(S.zr0, 1), zt0), z1 = min(S.zr1, zt1);
-            // the right strips start after the left ones where the two would meet (narrow grids)
-            const int x0 = max(k == 1 && pml ? max(S.xr0, a.nbd + 1) : S.xr0, xt0), x1 = min(S.xr1, xt1);
+            const StripBox& S = a.sbox[(pml ? 0 : 3) + k];
+            const int z0 = max(S.zr0, zt0), z1 = min(S.zr1, zt1);
+            const int x0 = max(S.xr0, xt0), x1 = min(S.xr1, xt1);
             const bool any = z0 <= z1 && x0 <= x1;
             bz0[k] = z0; bx0[k] = x0;
             bnz[k] = any ? z1 - z0 + 1 : 1;
             bcnt[k] = any ? (z1 - z0 + 1) * (x1 - x0 + 1) : 0;
-            const long long plane = (long long)S.rows * S.cols * a.it;
+            const long long plane = (long long)(S.rows * S.cols) * a.it;
             bxs[k] = a.strip[S.sx] + plane;
             bzs[k] = a.strip[S.sz] + plane;
             brows[k] = S.rows;
-            borg[k] = (long long)S.zr0 + (long long)S.rows * S.xr0;   // strip offset = iz + rows ix - org
+            borg[k] = S.org;
         }
         const int nb = bcnt[0] + bcnt[1] + bcnt[2];
         // strip element e: its shared-memory offset in the field tile and its two values
@@ -447,8 +427,8 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             divmod_small(e, k == 0 ? bnz[0] : k == 1 ? bnz[1] : bnz[2], xq, zr);
             const int iz = (k == 0 ? bz0[0] : k == 1 ? bz0[1] : bz0[2]) + zr;
             const int ix = (k == 0 ? bx0[0] : k == 1 ? bx0[1] : bx0[2]) + xq;
-            const long long o = (long long)iz + (k == 0 ? brows[0] : k == 1 ? brows[1] : brows[2]) * ix -
-                                (k == 0 ? borg[0] : k == 1 ? borg[1] : borg[2]);
+            const int o = iz + (k == 0 ? brows[0] : k == 1 ? brows[1] : brows[2]) * ix -
+                          (k == 0 ? borg[0] : k == 1 ? borg[1] : borg[2]);
             vx = __ldg((k == 0 ? bxs[0] : k == 1 ? bxs[1] : bxs[2]) + o);
             vz = __ldg((k == 0 ? bzs[0] : k == 1 ? bzs[1] : bzs[2]) + o);
             off = (int)(SU(sux, iz - R.z0, ix - R.x0) - sux);
@@ -465,8 +445,8 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
             const int e = tid + q * kThreads;
             if (e < nb) bg_elem(e, boff[q], bvx[q], bvz[q]);
         }
-        Walk wu(tid, P2, kThreads);   // (pair row, column) of this thread's field items, in order
-        Walk wm(tid, M2, kThreads);   // the same for the material items
+        Walk wu(qU, rU, wq[0], wr[0], P2);   // (pair row, column) of this thread's field items, in order
+        Walk wm(qM, rM, wq[1], wr[1], M2);   // the same for the material items
         for (int u0 = tid, m0 = tid; u0 < NP || m0 < NMP; u0 += kU * kThreads, m0 += kM * kThreads) {
             float2 vx[kU], vz[kU], l[kM], m[kM];
 #pragma unroll
@@ -590,8 +570,7 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
 
     // ---- phase 1a: x-direction staggered products and dzx operands, by row pairs -----------
     {
-        const int PZ = TZe / 2;
-        Walk w1(tid, PZ, kThreads);
+        Walk w1(qP, rP, wq[2], wr[2], PZ);
         for (int i = tid; i < PZ * T.XW; i += kThreads, w1.next()) {
             const int z = 2 * w1.r, xl = w1.q;
             const int iz = R.z0 + z;
@@ -657,9 +636,8 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
     }
     // ---- phase 1b: z-direction staggered products and dxz operands, by row pairs -----------
     {
-        const int PZ = T.ZW / 2;
-        Walk w2(tid, PZ, kThreads);
-        for (int i = tid; i < PZ * TX; i += kThreads, w2.next()) {
+        Walk w2(qM, rM, wq[1], wr[1], M2);   // ZW = MZ
+        for (int i = tid; i < M2 * TX; i += kThreads, w2.next()) {
             const int L = 2 * w2.r - OM, x = w2.q;   // rows / half-point labels L, L+1
             const int ix = R.x0 + x;
             const int o = x * T.ZW + (L + OM);
@@ -737,9 +715,8 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
     const float2 rdx2 = f2s(rdx), rdz2 = f2s(rdz);
     float* const uxn = a.ux[a.cur ^ 1];
     float* const uzn = a.uz[a.cur ^ 1];
-    const int PZ2 = TZe / 2;
-    Walk wc(tid, PZ2, kThreads);
-    for (int cell = tid; cell < PZ2 * TX; cell += kThreads, wc.next()) {
+    Walk wc(qP, rP, wq[2], wr[2], PZ);
+    for (int cell = tid; cell < PZ * TX; cell += kThreads, wc.next()) {
         const int z = 2 * wc.r, x = wc.q;
         const int iz = R.z0 + z;
         const int ix = R.x0 + x;
@@ -1215,6 +1192,27 @@ void plan_tiles(StepArgs& a, bool band_top, int pml_run)
     a.tiles_t_x = a.izt < 1 ? a.tiles_b_x : 0;
     a.top_pass = 0;
     a.n_tiles = a.tiles_int_z * a.tiles_int_x + 2 * a.tiles_l_z * a.tiles_l_x + a.tiles_b_z * a.tiles_b_x;
+    for (int c = 0; c < 3; ++c) {
+        const TileDims T = tile_dims(a.norder, a.tdz[c], a.tdx[c]);
+        const int n[3] = {T.UZ / 2, T.MZ / 2, T.TZe / 2};
+        for (int d = 0; d < 3; ++d) {
+            a.wq[c][d] = kThreads / n[d];
+            a.wr[c][d] = kThreads % n[d];
+        }
+    }
+    const int nx = a.nx, nz = a.nz, nbd = a.nbd;
+    // a strip stored from (zr0, xr0), its rows from row 1 on and (xs: where it starts in x, past
+    // the stored origin for the right inner strip, which starts after the left one where the two
+    // would meet on narrow grids)
+    auto box = [](int zr0, int zr1, int xr0, int xs, int xr1, int rows, int cols, int sx, int sz) {
+        return StripBox{std::max(zr0, 1), zr1, xs, xr1, rows, cols, zr0 + rows * xr0, sx, sz};
+    };
+    a.sbox[0] = box(1, nz - nbd, 1, 1, nbd, nz - nbd, nbd, UXL_REG, UZL_REG);
+    a.sbox[1] = box(1, nz - nbd, nx - nbd + 1, std::max(nx - nbd + 1, nbd + 1), nx, nz - nbd, nbd, UXR_REG, UZR_REG);
+    a.sbox[2] = box(nz - nbd + 1, nz, 1, 1, nx, nbd, nx, UXB_REG, UZB_REG);
+    a.sbox[3] = box(1, nz, 1 - nbd, 1 - nbd, 0, nz, nbd, UXL_PML, UZL_PML);
+    a.sbox[4] = box(1, nz, nx + 1, nx + 1, nx + nbd, nz, nbd, UXR_PML, UZR_PML);
+    a.sbox[5] = box(nz + 1, nz + nbd, 1 - nbd, 1 - nbd, nx + nbd, nbd, nx + 2 * nbd, UXB_PML, UZB_PML);
 }
 
 cudaError_t set_coefficients(const float* stag, const float* coll)

@@ -35,6 +35,15 @@ struct DampCol {   // per column (x) or row (z): d*dt and dt*d' for the PML
     float r1;      // 1 / (1 + y)
 };
 
+// One background strip as a rectangle of the grid: rows zr0..zr1, columns xr0..xr1, stored as
+// strip[(iz - zr0) + rows * ((ix - xr0) + cols * it)] (time slowest) in strip arrays sx, sz.
+struct StripBox {
+    int zr0, zr1, xr0, xr1;
+    int rows, cols;
+    int org;        // zr0 + rows * xr0: the strip offset of (iz, ix) is iz + rows * ix - org
+    int sx, sz;
+};
+
 // A DampCol from d*dt and dt*d' (the reciprocals formed in double, rounded once).
 inline DampCol make_damp(float y, float dtdp)
 {
@@ -77,6 +86,13 @@ struct StepArgs {
     int top_pass;                       // 1: this launch is the top layer's (after the interior update)
     int n_tiles;                        // tiles of this launch (the top layer's alone when top_pass)
     int tdz[3], tdx[3];                 // tile rows / columns of the interior, side-PML and bottom-PML tiles
+    // per tile class: the block's stride (kThreads items) through the item grids of its phases as
+    // (pair rows, columns) steps, for the grids of P2 (field tile), M2 (material tile and the
+    // z-direction products) and TZe/2 (x-direction products and output cells) pair rows
+    int wq[3][3], wr[3][3];
+    // the background strips: [0..2] inner (left, right, bottom; removed from the absorbing
+    // layers' operator field), [3..5] outer (added to the regular field)
+    StripBox sbox[6];
     // receivers sampled in the same launch (0 when this step takes no sample)
     int nrcv;
     int sample_index;          // istp
