@@ -136,14 +136,16 @@ int rebuild(fdfk_batch* b)
     std::vector<int> live(n, 0), eoff(n + 1, 0), moff(n + 1, 0), foff(n + 1, 0), toff(n + 1, 0);
     size_t smem = 0;
     // fast-path segments re-planned for the whole batch: about two waves of resident warps over
-    // all members' work, 16..48 columns per segment (a member alone plans for itself only)
+    // all members' work, 16..96 columns per segment (a member alone plans for itself only; longer
+    // segments spend fewer columns re-priming the pipeline, but past two waves the last one runs
+    // partly empty)
     long long work = 0;
     for (const fdfk_session* s : b->members) work += (long long)s->p.nx * s->march.n_bands;
     const int slots = b->norder <= kMarchMaxOrder ? march_warp_slots(b->norder) : 0;
     int seg = kMarchSeg;
     if (slots > 0) {
         seg = (int)((work + 2LL * slots - 1) / (2LL * slots));
-        seg = seg < 16 ? 16 : seg > 48 ? 48 : seg;
+        seg = seg < 16 ? 16 : seg > 96 ? 96 : seg;
     }
     if (b->seg_len > 0) seg = b->seg_len;
     for (int i = 0; i < n; ++i) {
