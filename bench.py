@@ -450,6 +450,7 @@ def main():
 
     import torch
     import fdfk2d_gb300 as F
+    from fdfk2d_gb300 import replicas
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", init_method="env://")
@@ -459,8 +460,7 @@ def main():
 
     def barrier():
         torch.cuda.synchronize(dev)
-        if world > 1:
-            torch.distributed.barrier()
+        replicas.barrier()
 
     # ---- device-resident arm: material and the FK background (computed on the GPU) in HBM
     # before the timed region; time axis = warm-up + timed steps
@@ -490,12 +490,9 @@ def main():
     ms_int, ms_edge, ms = sess.advance_timed(K, 8)
     barrier()
     launches = F.kernel_launches() - n0
-    t_dev = torch.tensor([ms], device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t_dev, op=torch.distributed.ReduceOp.MAX)
-    ms = float(t_dev.item())
+    ms = replicas.max_over_ranks(ms, dev)        # the slowest replica's time
     ms_step = ms / K
-    value = cells * K * world / (ms / 1e3) / 1e6
+    value = replicas.whole_job_rate(cells * K, ms / 1e3) / 1e6
 
     cells_int, cells_edge = sess.cell_split()
     sess.close()
@@ -529,7 +526,8 @@ def main():
     t_e2e = time.perf_counter() - t0
     se.close()
     clk = clocks.stop()
-    e2e_value = cells * K * world / t_e2e / 1e6
+    t_e2e = replicas.max_over_ranks(t_e2e, dev)
+    e2e_value = replicas.whole_job_rate(cells * K, t_e2e) / 1e6
     h2d = (c_host.nbytes + bazs_e.nbytes + fl_e.nbytes + fr_e.nbytes + 2 * 4 * len(w["rx"])) / K
     d2h = (outx.nbytes + outz.nbytes) / K
     assert np.isfinite(outz).all()
