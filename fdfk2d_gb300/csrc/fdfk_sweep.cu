@@ -568,11 +568,22 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
         }
     }
 
-    // ---- phase 1a: x-direction staggered products and dzx operands, by row pairs -----------
+    // ---- phase 1: half-point products and mixed operands, by row pairs: the x-direction items
+    // (1a) and then the z-direction items (1b) in one loop, so that the block's last, partly
+    // filled round of items is shared by the two kinds instead of each having its own
     {
+        const int n1a = PZ * T.XW, n1b = M2 * TX;
         Walk w1(qP, rP, wq[2], wr[2], PZ);
-        for (int i = tid; i < PZ * T.XW; i += kThreads, w1.next()) {
+        // this thread's first 1b item: its first index at or past n1a in tid, tid + kThreads, ...
+        const int kb = tid < n1a ? (n1a - tid + kThreads - 1) / kThreads : 0;
+        int qb, rb;
+        divmod_small(tid + kb * kThreads - n1a, M2, qb, rb);
+        Walk w2(qb, rb, wq[1], wr[1], M2);   // ZW = MZ
+        for (int i = tid; i < n1a + n1b; i += kThreads) {
+          if (i < n1a) {
+            // ---- 1a: x-direction staggered products and dzx operands
             const int z = 2 * w1.r, xl = w1.q;
+            w1.next();
             const int iz = R.z0 + z;
             const int o = xl * TZe + z;
             // staggered products at label L = xl - NO (half point between columns L and L+1)
@@ -632,13 +643,10 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                 sts2(v1 + o, a1);
                 sts2(v4 + o, a4);
             }
-        }
-    }
-    // ---- phase 1b: z-direction staggered products and dxz operands, by row pairs -----------
-    {
-        Walk w2(qM, rM, wq[1], wr[1], M2);   // ZW = MZ
-        for (int i = tid; i < M2 * TX; i += kThreads, w2.next()) {
+          } else {
+            // ---- 1b: z-direction staggered products and dxz operands
             const int L = 2 * w2.r - OM, x = w2.q;   // rows / half-point labels L, L+1
+            w2.next();
             const int ix = R.x0 + x;
             const int o = x * T.ZW + (L + OM);
             if (L <= TZ + NO - 2) {   // labels read by the output cells: -NO .. TZ+NO-2
@@ -706,6 +714,7 @@ __device__ __forceinline__ void step_block(const StepArgs& a, int blk)
                 sts2(v2 + o, a2);
                 sts2(v3 + o, a3);
             }
+          }
         }
     }
     __syncthreads();
