@@ -816,9 +816,13 @@ int fdfk_autotune(const fdfk_params* p, const float* c, int steps, int* seg_len,
     // the three fastest shapes timed again in turn, three rounds, and the lowest total chosen (the
     // two kernels share the SMs, and a single short timing can misrank shapes a few percent apart)
     constexpr int kFinal = 3, kRounds = 3;
-    const int trials = 2 * ((int)segs.size() + 2) + 5 + kFinal * kRounds;
+    // every timed window at least kWindowMs long (short windows of small models misrank shapes):
+    // `steps` steps, or more (up to kMaxSteps) where a step is short; the scratch session's time
+    // index restarts for every candidate, so its record covers one candidate's steps
+    constexpr float kWindowMs = 4.0f;
+    const int kMaxSteps = std::max(steps, 1000);
     fdfk_params q = *p;
-    q.nt = trials * (2 * steps + 2) + 1;
+    q.nt = 2 * kMaxSteps + 4;
     fdfk_session* s = nullptr;
     int rc = fdfk_session_create(&q, c, &s);
     if (rc) return rc;
@@ -838,22 +842,30 @@ int fdfk_autotune(const fdfk_params* p, const float* c, int steps, int* seg_len,
     for (int t = 0; t <= q.nt; ++t) s->have_bg[t] = 1;
     CK(cudaEventCreate(&g.e0));
     CK(cudaEventCreate(&g.e1));
+    int nsteps = steps;
     auto time_it = [&](int seg, int run, float& ms) -> int {
         int r = fdfk_session_set_tuning(s, seg, run);
         if (r) return r;
+        s->it = 0;   // zero state and background: the values, and so the time index, do not matter
         if ((r = fdfk_session_advance(s, 2))) return r;   // warm-up (first launches of a shape)
         ms = 1e30f;
         for (int rep = 0; rep < 2; ++rep) {
             float t = 0.f;
             CK(cudaEventRecord(g.e0, s->stream));
-            if ((r = fdfk_session_advance(s, steps))) return r;
+            if ((r = fdfk_session_advance(s, nsteps))) return r;
             CK(cudaEventRecord(g.e1, s->stream));
             CK(cudaEventSynchronize(g.e1));
             CK(cudaEventElapsedTime(&t, g.e0, g.e1));
-            ms = std::min(ms, t / steps);
+            ms = std::min(ms, t / nsteps);
         }
         return FDFK_OK;
     };
+    {   // the window length from one timing of the default shapes
+        float ms0 = 0.f;
+        if ((rc = time_it(0, 0, ms0))) return rc;
+        if (ms0 * steps < kWindowMs)
+            nsteps = std::min(kMaxSteps, (int)std::ceil(kWindowMs / std::max(ms0, 1e-4f)));
+    }
     // plus the shortest segments that fill exactly one and two waves of resident fast-path warps
     // (a partly filled last wave leaves SMs idle at the end of the step)
     if (s->march.n_bands > 0) {
