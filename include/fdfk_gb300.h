@@ -148,8 +148,10 @@ int fdfk_session_get_tuning(const fdfk_session* s, int* seg_len, int* pml_run);
  * shortest ones that fill one and two whole waves of fast-path warps;
  * absorbing-layer tile lengths 12..48) for sessions of parameters p and
  * material c on a scratch
- * session (zero state and background, `steps` timed steps per candidate,
- * CUDA events) and returns the fastest, for fdfk_session_set_tuning.
+ * session (zero state and background, CUDA events; each timed window
+ * `steps` steps, or more where that is shorter than 4 ms, up to
+ * max(steps, 1000)), re-times the three fastest in three interleaved rounds
+ * and returns the winner, for fdfk_session_set_tuning.
  */
 int fdfk_autotune(const fdfk_params* p, const float* c, int steps, int* seg_len, int* pml_run, float* ms_per_step);
 
